@@ -1,0 +1,231 @@
+/*
+ * msim.h - C ABI of the GB300 movement-sim per-tick path.
+ *
+ * The path: every tick each entity moves along its road toward the road end it
+ * heads for; at the end it picks the next road from the connection list with its
+ * own random state.  After the move, a spatial index over all entities is rebuilt
+ * (Morton key of the entity's tile, radix sort, tile ranges) and a radius
+ * neighbour query runs over it.
+ *
+ * Conventions
+ *  - Every function returns an int status (MSIM_OK on success).  On failure a
+ *    message is kept per thread and returned by msim_last_error().  No C++
+ *    exception crosses this ABI.
+ *  - Pointers are plain host pointers unless the name says "device".  Arrays are
+ *    indexed by entity id (0 .. num_entities-1) unless stated otherwise.
+ *  - A context is single-threaded: callers serialise calls on one context, as the
+ *    reference's worker thread does.  Separate contexts may run on separate threads.
+ *  - Work is queued on the context's own CUDA stream; msim_sync() waits for it and
+ *    reports device-side errors (bounded waits that gave up, indices out of range).
+ *
+ * Each entry point names the reference interface it replaces (file:line within
+ * COM8/movement-sim).
+ */
+#ifndef MSIM_H
+#define MSIM_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ---------------------------------------------------------- */
+enum {
+    MSIM_OK = 0,
+    MSIM_ERR_INVALID = 1, /* bad argument or malformed input */
+    MSIM_ERR_OOB = 2,     /* an index in map or entity data leaves its table */
+    MSIM_ERR_CUDA = 3,    /* a CUDA runtime call failed */
+    MSIM_ERR_TIMEOUT = 4, /* a bounded device-side wait gave up */
+    MSIM_ERR_NOMEM = 5,   /* device or host allocation failed */
+    MSIM_ERR_IO = 6       /* a file could not be read or written */
+};
+
+/* ---- random number generators -------------------------------------------- */
+/* xorshift128 with a uvec4 state, random_move.comp:725-746 (the reference's). */
+#define MSIM_RNG_XORSHIFT128 0u
+/* PCG32 (PCG-XSH-RR 64/32); state = {state_lo, state_hi, inc_lo, inc_hi}. */
+#define MSIM_RNG_PCG32 1u
+
+/* Heading word: bits 0..30 = road index (Entity.hpp:44 roadIndex), bit 31 set =
+ * the entity heads for the road's end, clear = for its start.  The reference
+ * keeps an explicit target position (Entity.hpp:41); it is always one endpoint of
+ * roads[roadIndex] (random_move.comp:787-819, Simulator.cpp:121-127). */
+#define MSIM_HEADING_TO_END 0x80000000u
+#define MSIM_HEADING_ROAD_MASK 0x7fffffffu
+
+/* Entity placement for msim_init_entities. */
+#define MSIM_PLACE_ROAD_START 0u       /* pos = road.start, as Simulator.cpp:121-127 */
+#define MSIM_PLACE_UNIFORM_FRACTION 1u /* pos = start + u*(end-start), u in [0,1) */
+
+/* msim_step flags */
+#define MSIM_STEP_NEIGHBOURS 1u /* rebuild the index and run the neighbour query */
+
+/* Unused neighbour slots in msim_get_neighbours output. */
+#define MSIM_NO_NEIGHBOUR 0xffffffffu
+
+/* ---- map ------------------------------------------------------------------- */
+/* Road graph, caller-owned host arrays (a view).  Layout of Map.hpp:12-48:
+ *   road_pos  : 4 floats per road  = start.x, start.y, end.x, end.y
+ *   road_conn : 4 uint32 per road  = connIndexStart, connCountStart,
+ *                                    connIndexEnd, connCountEnd
+ *   connections: connectionRoadIndexList
+ *   width/height: maxDistLat / maxDistLong (Map.cpp:42-52). */
+typedef struct msim_map {
+    uint32_t num_roads;
+    uint32_t num_connections;
+    const float* road_pos;
+    const uint32_t* road_conn;
+    const uint32_t* connections;
+    float width;
+    float height;
+} msim_map;
+
+/* A map owned by the library (from the JSON loader or the lattice generator). */
+typedef struct msim_map_buf msim_map_buf;
+
+/* Replaces Map::load_from_file (src/sim/Map.cpp:28-150).  Numbers are read as
+ * doubles and rounded to float; roads of zero length are skipped, as Map.cpp:124-128
+ * does (connection indices are kept as written).  Missing fields -> MSIM_ERR_INVALID. */
+int msim_map_load_json(const char* path, msim_map_buf** out);
+
+/* Synthetic L x L intersection lattice in the format of map/generate_map.py:234-258
+ * (one connection list per node, roads ending at the node listed twice, count =
+ * distinct incident roads, lists in ascending road id).  Nodes at spacing*(a,b) +
+ * uniform(-jitter, jitter) + jitter, edges kept with probability keep_prob, the
+ * largest component retained; every draw comes from splitmix64(seed, stream, i). */
+int msim_map_generate_lattice(uint32_t side, uint64_t seed, float spacing, float jitter,
+                              float keep_prob, msim_map_buf** out);
+
+/* Fills *out with pointers into buf (valid until msim_map_free). */
+int msim_map_view(const msim_map_buf* buf, msim_map* out);
+
+/* Writes the reference JSON map format (map/generate_map.py:152-160 to_json). */
+int msim_map_write_json(const msim_map* map, const char* path);
+
+void msim_map_free(msim_map_buf* buf);
+
+/* Checks a map the way msim_create does: every connection entry < num_roads, and
+ * for each road end with count >= 2, connIndex + count <= num_connections (the
+ * ranged draw of random_move.comp:743-746 can return count itself; index
+ * num_connections reads a pad entry equal to the last connection). */
+int msim_map_validate(const msim_map* map);
+
+/* ---- simulation context ---------------------------------------------------- */
+typedef struct msim_ctx msim_ctx;
+
+typedef struct msim_params {
+    uint32_t num_entities;    /* MAX_ENTITIES, Simulator.hpp:33 */
+    uint32_t rng_kind;        /* MSIM_RNG_* */
+    float dt;                 /* seconds per tick; 1.0 reproduces SPEED per dispatch */
+    float radius;             /* COLLISION_RADIUS, Simulator.hpp:43 */
+    uint32_t cap;             /* neighbours kept per entity, ascending id (0 = count only) */
+    float cell_size;          /* spatial tile side in metres; 0 = automatic */
+    uint32_t resort_interval; /* ticks between re-orderings of the entity state; 0 = automatic */
+    uint32_t flags;           /* reserved, must be 0 */
+} msim_params;
+
+typedef struct msim_init {
+    uint64_t seed;
+    uint32_t placement; /* MSIM_PLACE_* */
+    float speed_min;    /* per-entity speed drawn uniformly from [speed_min, speed_max] */
+    float speed_max;    /* (1.4, 1.4) with dt = 1 reproduces SPEED, random_move.comp:750 */
+} msim_init;
+
+/* Replaces Simulator::init (src/sim/Simulator.cpp:44-106): copies the map to the
+ * device (with one pad connection entry), allocates entity, index and neighbour
+ * buffers.  Entities start zeroed; call msim_init_entities or msim_set_entities. */
+int msim_create(const msim_map* map, const msim_params* params, msim_ctx** out);
+
+/* Replaces Simulator::~Simulator (Simulator.cpp:37-41); frees device memory. */
+int msim_destroy(msim_ctx* ctx);
+
+/* Replaces Simulator::add_entities (Simulator.cpp:114-129) and the random state of
+ * Entity.cpp:44-49 with a deterministic initializer from init->seed, then builds
+ * the tick-0 index (the reference's first dispatch inserts every entity into its
+ * quad tree, random_move.comp:863-867). */
+int msim_init_entities(msim_ctx* ctx, const msim_init* init);
+
+/* Replaces the host->device upload of the entity buffer (Simulator.cpp:189-193).
+ * pos: 2N floats, heading: N words, rng: 4N words, speed: N floats (speed may be
+ * NULL for 1.4 m per tick at dt = 1).  Builds the tick-0 index. */
+int msim_set_entities(msim_ctx* ctx, const float* pos, const uint32_t* heading,
+                      const uint32_t* rng, const float* speed);
+
+/* Per-road speed factors (num_roads floats, default 1): step = speed*factor*dt. */
+int msim_set_road_factors(msim_ctx* ctx, const float* factors);
+
+/* Replaces the per-tick pair of dispatches of Simulator::sim_tick
+ * (Simulator.cpp:213-237; random_move.comp:860-879): runs `ticks` ticks.  Without
+ * MSIM_STEP_NEIGHBOURS only the move runs (several ticks per launch); with it every
+ * tick is move, index rebuild, neighbour query.  Asynchronous. */
+int msim_step(msim_ctx* ctx, uint32_t ticks, uint32_t flags);
+
+/* Waits for queued work (the fence wait inside kp::Sequence::eval) and reports
+ * device-side errors recorded since the last call. */
+int msim_sync(msim_ctx* ctx);
+
+/* Replaces the device->host readback of the entity buffer (Simulator.cpp:248-263):
+ * any pointer may be NULL.  Synchronous. */
+int msim_get_state(msim_ctx* ctx, float* pos, uint32_t* heading, uint32_t* rng, float* speed);
+
+/* Result of the last neighbour tick (replaces the collision effect of
+ * random_move.comp:545-562).  count[i] = |{j != i : |dx|<=R, |dy|<=R, dist<R}|;
+ * idx (N*cap words, may be NULL) holds the min(count, cap) smallest such j in
+ * ascending order, the rest MSIM_NO_NEIGHBOUR.  Synchronous. */
+int msim_get_neighbours(msim_ctx* ctx, uint32_t* count, uint32_t* idx);
+
+/* debugData[1] of the last neighbour tick (random_move.comp:548): pairs j < i. */
+int msim_get_collision_pairs(msim_ctx* ctx, uint64_t* pairs);
+
+/* Writes n (= num_entities) 64-byte records in the layout of Entity.hpp:33-46
+ * (color, randomState, pos, target, direction, roadIndex, initialized) for
+ * Simulator::get_entities (Simulator.cpp:143-147).  color is green, or blue when
+ * the entity had a neighbour in the last neighbour tick (random_move.comp:545-549,
+ * 876); direction is recomputed from pos and target. */
+int msim_export_entities_aos(msim_ctx* ctx, void* out, size_t n);
+
+/* Number of ticks run since msim_create (one tick = move [+ collision]). */
+int msim_get_tick(msim_ctx* ctx, uint64_t* tick);
+
+/* Device-side timing of the context's kernels (CUDA events on its stream). */
+int msim_set_profiling(msim_ctx* ctx, int enable);
+int msim_reset_kernel_stats(msim_ctx* ctx);
+/* kernel: 0 .. msim_kernel_count()-1.  Synchronises the context's stream. */
+int msim_get_kernel_stats(msim_ctx* ctx, uint32_t kernel, uint64_t* launches, double* total_ms);
+uint32_t msim_kernel_count(void);
+const char* msim_kernel_name(uint32_t kernel);
+
+/* Events on the context's stream around a region of queued work (bench timing). */
+int msim_timer_begin(msim_ctx* ctx);
+int msim_timer_end(msim_ctx* ctx, float* ms);
+
+/* Page-locked host memory for copies inside timed regions. */
+int msim_host_alloc(size_t bytes, void** out);
+int msim_host_free(void* ptr);
+
+/* Resolved configuration of a context (for reports). */
+typedef struct msim_info {
+    uint32_t num_entities;
+    uint32_t num_roads;
+    uint32_t num_connections;
+    uint32_t tiles_x;
+    uint32_t tiles_y;
+    uint32_t key_bits;
+    uint32_t sort_passes;
+    uint32_t resort_interval;
+    float cell_size;
+    uint32_t cap;
+    uint64_t device_bytes;
+} msim_info;
+int msim_get_info(msim_ctx* ctx, msim_info* out);
+
+const char* msim_last_error(void);
+const char* msim_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MSIM_H */

@@ -1,0 +1,260 @@
+"""GB300-native per-tick path of movement-sim: Python bindings over the C ABI.
+
+Import with ``importlib.import_module("movement-sim_gb300")`` (the directory name
+carries a hyphen).  Everything here calls libmsim.so through include/msim.h;
+there is no CPU fallback.
+
+* :class:`RoadMap` - a road graph in the reference map layout (Map.hpp:12-48):
+  the JSON loader of Map.cpp:28-150, the writer of map/generate_map.py:152-160
+  and the synthetic lattice generator.
+* :class:`Simulation` - one device context (Simulator.cpp:44-106 init, sim_tick
+  213-279): entity set-up, ticks, state/neighbour/entity exports.
+"""
+from __future__ import annotations
+
+import ctypes
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _capi
+from ._capi import (HEADING_ROAD_MASK, HEADING_TO_END, NO_NEIGHBOUR, PLACE_ROAD_START,  # noqa: F401
+                    PLACE_UNIFORM_FRACTION, RNG_PCG32, RNG_XORSHIFT128, MsimError, check, lib)
+
+__all__ = ["RoadMap", "Simulation", "MsimError", "ENTITY_DTYPE", "RNG_XORSHIFT128", "RNG_PCG32",
+           "HEADING_TO_END", "HEADING_ROAD_MASK", "NO_NEIGHBOUR", "lib"]
+
+# Entity.hpp:33-46 (64-byte packed record)
+ENTITY_DTYPE = np.dtype([("color", "<f4", (4,)), ("randomState", "<u4", (4,)), ("pos", "<f4", (2,)),
+                         ("target", "<f4", (2,)), ("direction", "<f4", (2,)), ("roadIndex", "<u4"),
+                         ("initialized", "<u4")])
+assert ENTITY_DTYPE.itemsize == 64
+
+_RNG_KINDS = {"xorshift128": RNG_XORSHIFT128, "pcg32": RNG_PCG32}
+
+
+def _ptr(a, ctype):
+    return a.ctypes.data_as(ctypes.POINTER(ctype)) if a is not None else None
+
+
+@dataclass
+class RoadMap:
+    """Road graph: road_pos (R,4) float32 start.x, start.y, end.x, end.y; road_conn (R,4)
+    uint32 connIndexStart, connCountStart, connIndexEnd, connCountEnd; connections (C,)
+    uint32 (connectionRoadIndexList); width/height = maxDistLat/maxDistLong."""
+
+    road_pos: np.ndarray
+    road_conn: np.ndarray
+    connections: np.ndarray
+    width: float
+    height: float
+
+    def __post_init__(self):
+        self.road_pos = np.ascontiguousarray(self.road_pos, dtype=np.float32).reshape(-1, 4)
+        self.road_conn = np.ascontiguousarray(self.road_conn, dtype=np.uint32).reshape(-1, 4)
+        self.connections = np.ascontiguousarray(self.connections, dtype=np.uint32).reshape(-1)
+        self.width = float(np.float32(self.width))
+        self.height = float(np.float32(self.height))
+
+    @property
+    def num_roads(self) -> int:
+        return int(self.road_pos.shape[0])
+
+    def view(self) -> _capi.MsimMap:
+        m = _capi.MsimMap()
+        m.num_roads = self.num_roads
+        m.num_connections = int(self.connections.shape[0])
+        m.road_pos = _ptr(self.road_pos, ctypes.c_float)
+        m.road_conn = _ptr(self.road_conn, ctypes.c_uint32)
+        m.connections = _ptr(self.connections, ctypes.c_uint32)
+        m.width = self.width
+        m.height = self.height
+        return m
+
+    @classmethod
+    def _from_buf(cls, buf: ctypes.c_void_p) -> "RoadMap":
+        try:
+            v = _capi.MsimMap()
+            check(lib().msim_map_view(buf, ctypes.byref(v)))
+            R, C = v.num_roads, v.num_connections
+            pos = np.ctypeslib.as_array(v.road_pos, shape=(max(R, 1) * 4,))[: R * 4].copy() if R else np.zeros(0)
+            conn = np.ctypeslib.as_array(v.road_conn, shape=(max(R, 1) * 4,))[: R * 4].copy() if R else np.zeros(0)
+            cl = np.ctypeslib.as_array(v.connections, shape=(C,)).copy() if C else np.zeros(0, np.uint32)
+            return cls(pos, conn, cl, v.width, v.height)
+        finally:
+            lib().msim_map_free(buf)
+
+    @classmethod
+    def load_json(cls, path: str) -> "RoadMap":
+        """Map::load_from_file (Map.cpp:28-150)."""
+        buf = ctypes.c_void_p()
+        check(lib().msim_map_load_json(str(path).encode(), ctypes.byref(buf)))
+        return cls._from_buf(buf)
+
+    @classmethod
+    def lattice(cls, side: int, seed: int, spacing: float = 50.0, jitter: float = 10.0,
+                keep_prob: float = 0.9) -> "RoadMap":
+        """Synthetic side x side intersection lattice in the reference map format."""
+        buf = ctypes.c_void_p()
+        check(lib().msim_map_generate_lattice(side, seed, spacing, jitter, keep_prob, ctypes.byref(buf)))
+        return cls._from_buf(buf)
+
+    def write_json(self, path: str) -> None:
+        v = self.view()
+        check(lib().msim_map_write_json(ctypes.byref(v), str(path).encode()))
+
+    def validate(self) -> None:
+        v = self.view()
+        check(lib().msim_map_validate(ctypes.byref(v)))
+
+
+class Simulation:
+    """One simulation context on the current CUDA device.
+
+    Reference mode (random_move.comp as written): rng="xorshift128", dt=1.0,
+    speeds 1.4 (init_entities(speed=(1.4, 1.4))), radius 10.
+    """
+
+    def __init__(self, road_map: RoadMap, num_entities: int, *, rng: str = "xorshift128", dt: float = 1.0,
+                 radius: float = 10.0, cap: int = 64, cell_size: float = 0.0, resort_interval: int = 0):
+        self.map = road_map
+        self.n = int(num_entities)
+        self.cap = int(cap)
+        self.rng_kind = _RNG_KINDS[rng]
+        p = _capi.MsimParams(num_entities=self.n, rng_kind=self.rng_kind, dt=dt, radius=radius, cap=self.cap,
+                             cell_size=cell_size, resort_interval=resort_interval, flags=0)
+        self._ctx = ctypes.c_void_p()
+        v = road_map.view()
+        check(lib().msim_create(ctypes.byref(v), ctypes.byref(p), ctypes.byref(self._ctx)))
+
+    # -- lifecycle ---------------------------------------------------------
+    def close(self) -> None:
+        if getattr(self, "_ctx", None) is not None and self._ctx.value:
+            lib().msim_destroy(self._ctx)
+            self._ctx = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    # -- entities ----------------------------------------------------------
+    def init_entities(self, seed: int, placement: str = "start", speed=(1.4, 1.4)) -> None:
+        pl = {"start": PLACE_ROAD_START, "fraction": PLACE_UNIFORM_FRACTION}[placement]
+        ini = _capi.MsimInit(seed=seed, placement=pl, speed_min=speed[0], speed_max=speed[1])
+        check(lib().msim_init_entities(self._ctx, ctypes.byref(ini)))
+
+    def set_entities(self, pos, heading, rng, speed=None) -> None:
+        pos = np.ascontiguousarray(pos, dtype=np.float32).reshape(self.n, 2)
+        heading = np.ascontiguousarray(heading, dtype=np.uint32).reshape(self.n)
+        rng = np.ascontiguousarray(rng, dtype=np.uint32).reshape(self.n, 4)
+        if speed is not None:
+            speed = np.ascontiguousarray(speed, dtype=np.float32).reshape(self.n)
+        check(lib().msim_set_entities(self._ctx, _ptr(pos, ctypes.c_float), _ptr(heading, ctypes.c_uint32),
+                                      _ptr(rng, ctypes.c_uint32), _ptr(speed, ctypes.c_float)))
+
+    def set_road_factors(self, factors) -> None:
+        f = np.ascontiguousarray(factors, dtype=np.float32).reshape(self.map.num_roads)
+        check(lib().msim_set_road_factors(self._ctx, _ptr(f, ctypes.c_float)))
+
+    # -- ticks ---------------------------------------------------------------
+    def step(self, ticks: int = 1, neighbours: bool = False) -> None:
+        check(lib().msim_step(self._ctx, ticks, _capi.STEP_NEIGHBOURS if neighbours else 0))
+
+    def sync(self) -> None:
+        check(lib().msim_sync(self._ctx))
+
+    @property
+    def tick(self) -> int:
+        t = ctypes.c_uint64()
+        check(lib().msim_get_tick(self._ctx, ctypes.byref(t)))
+        return t.value
+
+    # -- exports ---------------------------------------------------------------
+    def get_state(self, out=None):
+        """dict of pos (N,2) f32, heading (N,) u32, rng (N,4) u32, speed (N,) f32, by entity id."""
+        if out is None:
+            out = {"pos": np.empty((self.n, 2), np.float32), "heading": np.empty(self.n, np.uint32),
+                   "rng": np.empty((self.n, 4), np.uint32), "speed": np.empty(self.n, np.float32)}
+        check(lib().msim_get_state(self._ctx, _ptr(out.get("pos"), ctypes.c_float),
+                                   _ptr(out.get("heading"), ctypes.c_uint32), _ptr(out.get("rng"), ctypes.c_uint32),
+                                   _ptr(out.get("speed"), ctypes.c_float)))
+        return out
+
+    def get_neighbours(self, with_idx: bool = True):
+        count = np.empty(self.n, np.uint32)
+        idx = np.empty((self.n, self.cap), np.uint32) if (with_idx and self.cap) else None
+        check(lib().msim_get_neighbours(self._ctx, _ptr(count, ctypes.c_uint32), _ptr(idx, ctypes.c_uint32)))
+        return count, idx
+
+    def collision_pairs(self) -> int:
+        v = ctypes.c_uint64()
+        check(lib().msim_get_collision_pairs(self._ctx, ctypes.byref(v)))
+        return v.value
+
+    def export_entities(self) -> np.ndarray:
+        out = np.empty(self.n, ENTITY_DTYPE)
+        check(lib().msim_export_entities_aos(self._ctx, out.ctypes.data_as(ctypes.c_void_p), self.n))
+        return out
+
+    # -- reports / timing ------------------------------------------------------
+    def info(self) -> dict:
+        i = _capi.MsimInfo()
+        check(lib().msim_get_info(self._ctx, ctypes.byref(i)))
+        return {f: getattr(i, f) for f, _ in _capi.MsimInfo._fields_}
+
+    def set_profiling(self, on: bool) -> None:
+        check(lib().msim_set_profiling(self._ctx, 1 if on else 0))
+
+    def reset_kernel_stats(self) -> None:
+        check(lib().msim_reset_kernel_stats(self._ctx))
+
+    def kernel_stats(self) -> dict:
+        out = {}
+        for k in range(lib().msim_kernel_count()):
+            n = ctypes.c_uint64()
+            ms = ctypes.c_double()
+            check(lib().msim_get_kernel_stats(self._ctx, k, ctypes.byref(n), ctypes.byref(ms)))
+            if n.value:
+                out[lib().msim_kernel_name(k).decode()] = {"launches": n.value, "ms": ms.value}
+        return out
+
+    def timer_begin(self) -> None:
+        check(lib().msim_timer_begin(self._ctx))
+
+    def timer_end(self) -> float:
+        ms = ctypes.c_float()
+        check(lib().msim_timer_end(self._ctx, ctypes.byref(ms)))
+        return ms.value
+
+
+class PinnedBuffer:
+    """Page-locked host memory (cudaMallocHost) viewed as a numpy array."""
+
+    def __init__(self, shape, dtype):
+        self.dtype = np.dtype(dtype)
+        self.shape = tuple(shape) if isinstance(shape, (tuple, list)) else (int(shape),)
+        nbytes = int(np.prod(self.shape)) * self.dtype.itemsize
+        self._p = ctypes.c_void_p()
+        check(lib().msim_host_alloc(max(nbytes, 1), ctypes.byref(self._p)))
+        buf = (ctypes.c_char * max(nbytes, 1)).from_address(self._p.value)
+        self.array = np.frombuffer(buf, dtype=self.dtype, count=int(np.prod(self.shape))).reshape(self.shape)
+
+    def free(self):
+        if self._p.value:
+            self.array = None
+            lib().msim_host_free(self._p)
+            self._p = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass

@@ -1,0 +1,730 @@
+// C ABI of the movement-sim per-tick path: context lifecycle, tick orchestration
+// on the context's CUDA stream, exports back to the reference's layouts.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "msim_internal.h"
+#include "msim_kernels.cuh"
+
+namespace msim {
+
+static thread_local std::string g_last_error;
+
+void set_error(const std::string& msg) { g_last_error = msg; }
+int fail(int code, const std::string& msg) {
+    g_last_error = msg;
+    return code;
+}
+
+enum KernelId : uint32_t {
+    K_INIT = 0,
+    K_STEP,        // one tick + key + digit histogram (neighbour ticks)
+    K_STEP_MULTI,  // several move-only ticks per launch
+    K_HIST_SCAN,
+    K_SORT_PASS,
+    K_RANGES,
+    K_QUERY,
+    K_PERMUTE,
+    K_EXPORT,
+    K_COUNT
+};
+static const char* const kKernelNames[K_COUNT] = {"k_init",   "k_step",  "k_step_multi", "k_hist_scan", "k_onesweep",
+                                                  "k_ranges", "k_query", "k_permute",    "k_export"};
+
+}  // namespace msim
+
+using namespace msim;
+
+struct msim_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    msim_params params{};
+    uint32_t n = 0, R = 0, C = 0;
+    float world_w = 0.f, world_h = 0.f;
+    // map
+    float4* road_pos = nullptr;
+    uint4* road_conn = nullptr;
+    uint32_t* conn = nullptr;
+    float* factor = nullptr;
+    // entity state, double-buffered for re-ordering
+    EntityState st[2]{};
+    int cur = 0;
+    // spatial index
+    uint32_t* key = nullptr;
+    uint32_t* sk[2] = {nullptr, nullptr};
+    uint32_t* sv[2] = {nullptr, nullptr};
+    uint32_t* hist = nullptr;
+    uint32_t* digit_off = nullptr;
+    uint32_t* lookback = nullptr;
+    uint32_t* tickets = nullptr;
+    uint2* ranges = nullptr;
+    size_t ranges_count = 0;
+    uint32_t sort_tiles = 0;
+    const uint32_t* sorted_key = nullptr;
+    const uint32_t* sorted_slot = nullptr;
+    bool have_sort = false;
+    // neighbours
+    uint32_t* nbr_count = nullptr;
+    uint32_t* nbr_list = nullptr;
+    unsigned long long* pairs = nullptr;
+    bool have_nbr = false;
+    uint32_t* err = nullptr;
+    TileGrid grid{};
+    uint32_t passes = 1;
+    uint32_t resort = 16;
+    uint32_t since_permute = 0;
+    int step_blocks = 1;
+    uint64_t tick = 0;
+    size_t device_bytes = 0;
+    std::vector<void*> allocs;
+    void* stage = nullptr;
+    size_t stage_bytes = 0;
+    // profiling
+    bool profiling = false;
+    struct Pending {
+        uint32_t kernel;
+        cudaEvent_t a, b;
+    };
+    std::vector<Pending> pending;
+    std::vector<cudaEvent_t> pool;
+    uint64_t launches[K_COUNT] = {};
+    double ms[K_COUNT] = {};
+    cudaEvent_t t0 = nullptr, t1 = nullptr;
+    bool timer_open = false;
+
+    DeviceMap dmap() const {
+        DeviceMap m;
+        m.road_pos = road_pos;
+        m.road_conn = road_conn;
+        m.conn = conn;
+        m.factor = factor;
+        m.num_roads = R;
+        m.num_conn = C;
+        return m;
+    }
+};
+
+namespace {
+
+int cuda_fail(cudaError_t e, const char* what) {
+    return fail(MSIM_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define CK(expr, what)                                   \
+    do {                                                 \
+        cudaError_t e_ = (expr);                         \
+        if (e_ != cudaSuccess) return cuda_fail(e_, what); \
+    } while (0)
+
+template <typename T>
+int dalloc(msim_ctx* c, T** p, size_t count) {
+    *p = nullptr;
+    if (count == 0) count = 1;
+    void* raw = nullptr;
+    cudaError_t e = cudaMalloc(&raw, count * sizeof(T));
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return fail(MSIM_ERR_NOMEM, "cudaMalloc of " + std::to_string(count * sizeof(T)) + " bytes failed: " +
+                                        cudaGetErrorString(e));
+    }
+    c->allocs.push_back(raw);
+    c->device_bytes += count * sizeof(T);
+    *p = static_cast<T*>(raw);
+    return MSIM_OK;
+}
+
+void free_all(msim_ctx* c) {
+    for (void* p : c->allocs) cudaFree(p);
+    c->allocs.clear();
+    if (c->stage) cudaFree(c->stage);
+    c->stage = nullptr;
+    for (auto& pd : c->pending) {
+        c->pool.push_back(pd.a);
+        c->pool.push_back(pd.b);
+    }
+    c->pending.clear();
+    for (cudaEvent_t e : c->pool) cudaEventDestroy(e);
+    c->pool.clear();
+    if (c->t0) cudaEventDestroy(c->t0);
+    if (c->t1) cudaEventDestroy(c->t1);
+    if (c->stream) cudaStreamDestroy(c->stream);
+}
+
+cudaEvent_t pool_event(msim_ctx* c) {
+    if (!c->pool.empty()) {
+        cudaEvent_t e = c->pool.back();
+        c->pool.pop_back();
+        return e;
+    }
+    cudaEvent_t e = nullptr;
+    cudaEventCreate(&e);
+    return e;
+}
+
+// Records an event pair around one launch when profiling is on.
+struct Prof {
+    msim_ctx* c;
+    uint32_t k;
+    cudaEvent_t a = nullptr;
+    Prof(msim_ctx* ctx, uint32_t kernel) : c(ctx), k(kernel) {
+        if (c->profiling) {
+            a = pool_event(c);
+            cudaEventRecord(a, c->stream);
+        }
+    }
+    ~Prof() {
+        if (a) {
+            cudaEvent_t b = pool_event(c);
+            cudaEventRecord(b, c->stream);
+            c->pending.push_back({k, a, b});
+        }
+    }
+};
+
+int drain_profile(msim_ctx* c) {
+    if (c->pending.empty()) return MSIM_OK;
+    CK(cudaStreamSynchronize(c->stream), "cudaStreamSynchronize");
+    for (auto& pd : c->pending) {
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, pd.a, pd.b);
+        c->launches[pd.kernel]++;
+        c->ms[pd.kernel] += ms;
+        c->pool.push_back(pd.a);
+        c->pool.push_back(pd.b);
+    }
+    c->pending.clear();
+    return MSIM_OK;
+}
+
+int ensure_stage(msim_ctx* c, size_t bytes) {
+    if (c->stage_bytes >= bytes) return MSIM_OK;
+    if (c->stage) cudaFree(c->stage);
+    c->stage = nullptr;
+    c->stage_bytes = 0;
+    cudaError_t e = cudaMalloc(&c->stage, bytes);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        c->stage = nullptr;
+        return fail(MSIM_ERR_NOMEM, "cudaMalloc of export staging (" + std::to_string(bytes) + " bytes) failed");
+    }
+    c->stage_bytes = bytes;
+    return MSIM_OK;
+}
+
+EntityState& cur_state(msim_ctx* c) { return c->st[c->cur]; }
+
+StepLaunch step_args(msim_ctx* c, uint32_t ticks, bool key) {
+    StepLaunch a;
+    a.map = c->dmap();
+    a.st = cur_state(c);
+    a.n = c->n;
+    a.dt = c->params.dt;
+    a.ticks = ticks;
+    a.rng_kind = c->params.rng_kind;
+    a.key = key ? c->key : nullptr;
+    a.hist = c->hist;
+    a.grid = c->grid;
+    a.passes = c->passes;
+    a.err = c->err;
+    a.blocks = c->step_blocks;
+    return a;
+}
+
+// key + histogram (of the current positions, or after one move tick) + radix sort
+int sort_entities(msim_ctx* c, uint32_t move_ticks) {
+    CK(cudaMemsetAsync(c->hist, 0, sizeof(uint32_t) * kMaxPasses * kRadix, c->stream), "memset hist");
+    {
+        Prof p(c, K_STEP);
+        CK(launch_step(c->stream, step_args(c, move_ticks, true)), "k_step");
+    }
+    {
+        Prof p(c, K_HIST_SCAN);
+        CK(launch_hist_scan(c->stream, c->hist, c->digit_off, c->passes), "k_hist_scan");
+    }
+    CK(cudaMemsetAsync(c->lookback, 0, sizeof(uint32_t) * (size_t)c->passes * c->sort_tiles * kRadix, c->stream),
+       "memset lookback");
+    CK(cudaMemsetAsync(c->tickets, 0, sizeof(uint32_t) * kMaxPasses, c->stream), "memset tickets");
+    for (uint32_t ps = 0; ps < c->passes; ps++) {
+        const uint32_t* kin = ps == 0 ? c->key : c->sk[(ps - 1) & 1];
+        const uint32_t* vin = ps == 0 ? nullptr : c->sv[(ps - 1) & 1];
+        Prof p(c, K_SORT_PASS);
+        CK(launch_onesweep(c->stream, kin, vin, c->sk[ps & 1], c->sv[ps & 1], c->n, 8u * ps,
+                           c->digit_off + ps * kRadix, c->lookback + (size_t)ps * c->sort_tiles * kRadix,
+                           c->tickets + ps, c->err),
+           "k_onesweep");
+    }
+    c->sorted_key = c->sk[(c->passes - 1) & 1];
+    c->sorted_slot = c->sv[(c->passes - 1) & 1];
+    c->have_sort = true;
+    return MSIM_OK;
+}
+
+int permute_state(msim_ctx* c) {
+    Prof p(c, K_PERMUTE);
+    CK(launch_permute(c->stream, c->sorted_slot, c->st[c->cur], c->st[1 - c->cur], c->n), "k_permute");
+    c->cur = 1 - c->cur;
+    c->have_sort = false;
+    c->since_permute = 0;
+    return MSIM_OK;
+}
+
+// tick-0 index: the reference's first dispatch only inserts every entity into its
+// tree (random_move.comp:863-867); here: sort by tile and re-order the state.
+int build_index(msim_ctx* c) {
+    c->have_nbr = false;
+    if (c->n == 0) return MSIM_OK;
+    int rc = sort_entities(c, 0);
+    if (rc != MSIM_OK) return rc;
+    return permute_state(c);
+}
+
+int neighbour_tick(msim_ctx* c) {
+    int rc;
+    if (c->have_sort && c->since_permute >= c->resort) {
+        rc = permute_state(c);
+        if (rc != MSIM_OK) return rc;
+    }
+    rc = sort_entities(c, 1);
+    if (rc != MSIM_OK) return rc;
+    CK(cudaMemsetAsync(c->ranges, 0, sizeof(uint2) * c->ranges_count, c->stream), "memset ranges");
+    {
+        Prof p(c, K_RANGES);
+        CK(launch_ranges(c->stream, c->sorted_key, c->n, c->ranges), "k_ranges");
+    }
+    CK(cudaMemsetAsync(c->pairs, 0, sizeof(unsigned long long), c->stream), "memset pairs");
+    {
+        Prof p(c, K_QUERY);
+        CK(launch_query(c->stream, c->params.cap, c->sorted_slot, cur_state(c).pos, cur_state(c).slot_id, c->ranges,
+                        c->grid, c->n, c->nbr_count, c->nbr_list, c->pairs),
+           "k_query");
+    }
+    c->have_nbr = true;
+    c->since_permute++;
+    return MSIM_OK;
+}
+
+int check_ctx(msim_ctx* c) {
+    if (!c) return fail(MSIM_ERR_INVALID, "context is NULL");
+    cudaError_t e = cudaSetDevice(c->device);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaSetDevice");
+    return MSIM_OK;
+}
+
+int sync_and_check(msim_ctx* c) {
+    CK(cudaStreamSynchronize(c->stream), "cudaStreamSynchronize");
+    uint32_t h = 0;
+    CK(cudaMemcpy(&h, c->err, sizeof(h), cudaMemcpyDeviceToHost), "read device status");
+    if (h) {
+        CK(cudaMemset(c->err, 0, sizeof(uint32_t)), "clear device status");
+        if (h & kErrTimeout)
+            return fail(MSIM_ERR_TIMEOUT, "a bounded device wait (radix sort look-back) gave up; results of the tick are invalid");
+        return fail(MSIM_ERR_OOB, "a device-side index check failed (road or connection index out of range)");
+    }
+    return MSIM_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* msim_last_error(void) { return g_last_error.c_str(); }
+const char* msim_version(void) { return "msim-gb300 0.1 (sm_103a)"; }
+
+uint32_t msim_kernel_count(void) { return K_COUNT; }
+const char* msim_kernel_name(uint32_t k) { return k < K_COUNT ? kKernelNames[k] : ""; }
+
+int msim_create(const msim_map* map, const msim_params* params, msim_ctx** out) {
+    if (!out) return fail(MSIM_ERR_INVALID, "out is NULL");
+    *out = nullptr;
+    if (!map || !params) return fail(MSIM_ERR_INVALID, "map or params is NULL");
+    int rc = validate_map(*map);
+    if (rc != MSIM_OK) return rc;
+    const msim_params& p = *params;
+    if (p.num_entities >= (1u << 30)) return fail(MSIM_ERR_INVALID, "num_entities must be < 2^30");
+    if (p.rng_kind > 1) return fail(MSIM_ERR_INVALID, "unknown rng_kind");
+    if (!std::isfinite(p.dt) || !(p.dt > 0.f)) return fail(MSIM_ERR_INVALID, "dt must be positive and finite");
+    if (!std::isfinite(p.radius) || p.radius < 0.f) return fail(MSIM_ERR_INVALID, "radius must be finite and >= 0");
+    if (p.cap > kMaxCap) return fail(MSIM_ERR_INVALID, "cap must be <= " + std::to_string(kMaxCap));
+    if (p.cell_size < 0.f || !std::isfinite(p.cell_size)) return fail(MSIM_ERR_INVALID, "cell_size must be >= 0");
+    if (p.flags != 0) return fail(MSIM_ERR_INVALID, "flags must be 0");
+
+    msim_ctx* c = new (std::nothrow) msim_ctx();
+    if (!c) return fail(MSIM_ERR_NOMEM, "out of host memory");
+    cudaError_t e = cudaGetDevice(&c->device);
+    if (e != cudaSuccess) {
+        delete c;
+        return cuda_fail(e, "cudaGetDevice");
+    }
+    c->params = p;
+    c->n = p.num_entities;
+    c->R = map->num_roads;
+    c->C = map->num_connections;
+    c->world_w = map->width;
+    c->world_h = map->height;
+
+    auto bail = [&](int code) {
+        free_all(c);
+        delete c;
+        return code;
+    };
+    e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) return bail(cuda_fail(e, "cudaStreamCreate"));
+    if (cudaEventCreate(&c->t0) != cudaSuccess || cudaEventCreate(&c->t1) != cudaSuccess)
+        return bail(fail(MSIM_ERR_CUDA, "cudaEventCreate failed"));
+
+    // ---- spatial grid ----
+    double maxc = std::max((double)c->world_w, (double)c->world_h);
+    for (uint64_t i = 0; i < 4ull * c->R; i++) maxc = std::max(maxc, std::fabs((double)map->road_pos[i]));
+    const double radius = p.radius;
+    // reach covers the rounding of |dx| in the predicate and of pos -/+ reach
+    const double reach = radius * (1.0 + 0x1p-20) + maxc * 0x1p-20 + 1e-30;
+    double cell = p.cell_size;
+    if (cell <= 0.0) {
+        double area = (double)c->world_w * (double)c->world_h;
+        cell = std::max(2.0 * reach, 4.0 * std::sqrt(area / std::max<double>(c->n, 1.0)));
+    }
+    cell = std::max(cell, 1e-3);
+    uint32_t bits = 1;
+    for (;;) {
+        double tx = std::ceil((double)c->world_w / cell), ty = std::ceil((double)c->world_h / cell);
+        tx = std::max(tx, 1.0);
+        ty = std::max(ty, 1.0);
+        double tmax = std::max(tx, ty);
+        bits = 1;
+        while ((double)(1u << bits) < tmax) bits++;
+        if (bits <= 11) {
+            c->grid.tiles_x = (uint32_t)tx;
+            c->grid.tiles_y = (uint32_t)ty;
+            break;
+        }
+        cell = std::max((double)c->world_w, (double)c->world_h) / 2048.0 * (1.0 + 1e-6);
+    }
+    c->grid.inv_cell = (float)(1.0 / cell);
+    c->grid.bits = bits;
+    c->grid.reach = (float)reach;
+    c->grid.radius = p.radius;
+    c->passes = (2 * bits + 7) / 8;
+    c->ranges_count = (size_t)1 << (2 * bits);
+    c->resort = p.resort_interval ? p.resort_interval : 16u;
+    c->sort_tiles = (uint32_t)((c->n + kSortTile - 1) / kSortTile);
+    if (c->sort_tiles == 0) c->sort_tiles = 1;
+
+    // ---- device buffers ----
+    const size_t n = c->n;
+    if ((rc = dalloc(c, &c->road_pos, c->R)) || (rc = dalloc(c, &c->road_conn, c->R)) ||
+        (rc = dalloc(c, &c->conn, (size_t)c->C + 1)))
+        return bail(rc);
+    for (int b = 0; b < 2; b++) {
+        if ((rc = dalloc(c, &c->st[b].pos, n)) || (rc = dalloc(c, &c->st[b].head, n)) ||
+            (rc = dalloc(c, &c->st[b].rng, n)) || (rc = dalloc(c, &c->st[b].speed, n)) ||
+            (rc = dalloc(c, &c->st[b].slot_id, n)) || (rc = dalloc(c, &c->sk[b], n)) || (rc = dalloc(c, &c->sv[b], n)))
+            return bail(rc);
+    }
+    if ((rc = dalloc(c, &c->key, n)) || (rc = dalloc(c, &c->hist, (size_t)kMaxPasses * kRadix)) ||
+        (rc = dalloc(c, &c->digit_off, (size_t)kMaxPasses * kRadix)) ||
+        (rc = dalloc(c, &c->lookback, (size_t)kMaxPasses * c->sort_tiles * kRadix)) ||
+        (rc = dalloc(c, &c->tickets, (size_t)kMaxPasses)) || (rc = dalloc(c, &c->ranges, c->ranges_count)) ||
+        (rc = dalloc(c, &c->nbr_count, n)) || (rc = dalloc(c, &c->pairs, 1)) || (rc = dalloc(c, &c->err, 1)))
+        return bail(rc);
+    if (p.cap > 0) {
+        size_t blocks = (n + kQueryThreads - 1) / kQueryThreads;
+        if ((rc = dalloc(c, &c->nbr_list, blocks * kQueryThreads * (size_t)p.cap))) return bail(rc);
+    }
+
+    // ---- map upload (connections + one pad entry equal to the last) ----
+    std::vector<uint32_t> conn(c->C + 1);
+    if (c->C) std::memcpy(conn.data(), map->connections, sizeof(uint32_t) * c->C);
+    conn[c->C] = c->C ? map->connections[c->C - 1] : 0u;
+    e = cudaMemcpy(c->road_pos, map->road_pos, sizeof(float4) * c->R, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(c->road_conn, map->road_conn, sizeof(uint4) * c->R, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(c->conn, conn.data(), sizeof(uint32_t) * (c->C + 1), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemset(c->err, 0, sizeof(uint32_t));
+    for (int b = 0; b < 2 && e == cudaSuccess; b++) {
+        e = cudaMemset(c->st[b].pos, 0, sizeof(float2) * std::max<size_t>(n, 1));
+        if (e == cudaSuccess) e = cudaMemset(c->st[b].head, 0, sizeof(uint32_t) * std::max<size_t>(n, 1));
+        if (e == cudaSuccess) e = cudaMemset(c->st[b].rng, 0, sizeof(uint4) * std::max<size_t>(n, 1));
+        if (e == cudaSuccess) e = cudaMemset(c->st[b].speed, 0, sizeof(float) * std::max<size_t>(n, 1));
+        if (e == cudaSuccess) e = cudaMemset(c->st[b].slot_id, 0, sizeof(uint32_t) * std::max<size_t>(n, 1));
+    }
+    if (e == cudaSuccess) e = configure_kernels(p.cap);
+    if (e != cudaSuccess) return bail(cuda_fail(e, "context set-up"));
+    c->step_blocks = step_blocks_for(c->device, c->n);
+    *out = c;
+    return MSIM_OK;
+}
+
+int msim_destroy(msim_ctx* c) {
+    if (!c) return MSIM_OK;
+    cudaSetDevice(c->device);
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    free_all(c);
+    delete c;
+    return MSIM_OK;
+}
+
+int msim_init_entities(msim_ctx* c, const msim_init* init) {
+    int rc = check_ctx(c);
+    if (rc != MSIM_OK) return rc;
+    if (!init) return fail(MSIM_ERR_INVALID, "init is NULL");
+    if (init->placement > 1) return fail(MSIM_ERR_INVALID, "unknown placement");
+    if (!std::isfinite(init->speed_min) || !std::isfinite(init->speed_max) || init->speed_max < init->speed_min)
+        return fail(MSIM_ERR_INVALID, "need finite speed_min <= speed_max");
+    c->cur = 0;
+    {
+        Prof p(c, K_INIT);
+        CK(launch_init_entities(c->stream, c->dmap(), c->st[0], c->n, c->params.rng_kind, init->seed, init->placement,
+                                init->speed_min, init->speed_max),
+           "k_init");
+    }
+    return build_index(c);
+}
+
+int msim_set_entities(msim_ctx* c, const float* pos, const uint32_t* heading, const uint32_t* rng,
+                      const float* speed) {
+    int rc = check_ctx(c);
+    if (rc != MSIM_OK) return rc;
+    if (c->n && (!pos || !heading || !rng)) return fail(MSIM_ERR_INVALID, "pos, heading and rng are required");
+    for (uint32_t i = 0; i < c->n; i++)
+        if ((heading[i] & MSIM_HEADING_ROAD_MASK) >= c->R)
+            return fail(MSIM_ERR_OOB, "heading of entity " + std::to_string(i) + " names road " +
+                                          std::to_string(heading[i] & MSIM_HEADING_ROAD_MASK) + " of " +
+                                          std::to_string(c->R));
+    c->cur = 0;
+    EntityState& s = c->st[0];
+    const size_t n = c->n;
+    if (n == 0) return MSIM_OK;
+    CK(cudaMemcpyAsync(s.pos, pos, sizeof(float2) * n, cudaMemcpyHostToDevice, c->stream), "upload pos");
+    CK(cudaMemcpyAsync(s.head, heading, sizeof(uint32_t) * n, cudaMemcpyHostToDevice, c->stream), "upload heading");
+    CK(cudaMemcpyAsync(s.rng, rng, sizeof(uint4) * n, cudaMemcpyHostToDevice, c->stream), "upload rng");
+    if (speed) {
+        CK(cudaMemcpyAsync(s.speed, speed, sizeof(float) * n, cudaMemcpyHostToDevice, c->stream), "upload speed");
+    } else {
+        std::vector<float> sp(n, 1.4f);
+        CK(cudaMemcpyAsync(s.speed, sp.data(), sizeof(float) * n, cudaMemcpyHostToDevice, c->stream), "upload speed");
+        CK(cudaStreamSynchronize(c->stream), "sync");
+    }
+    // entity i starts in slot i
+    CK(launch_iota(c->stream, s.slot_id, c->n), "k_iota");
+    return build_index(c);
+}
+
+int msim_set_road_factors(msim_ctx* c, const float* factors) {
+    int rc = check_ctx(c);
+    if (rc != MSIM_OK) return rc;
+    if (!factors) return fail(MSIM_ERR_INVALID, "factors is NULL");
+    for (uint32_t r = 0; r < c->R; r++)
+        if (!std::isfinite(factors[r])) return fail(MSIM_ERR_INVALID, "non-finite road factor");
+    if (!c->factor && (rc = dalloc(c, &c->factor, c->R))) return rc;
+    CK(cudaMemcpyAsync(c->factor, factors, sizeof(float) * c->R, cudaMemcpyHostToDevice, c->stream), "upload factors");
+    CK(cudaStreamSynchronize(c->stream), "sync");
+    return MSIM_OK;
+}
+
+int msim_step(msim_ctx* c, uint32_t ticks, uint32_t flags) {
+    int rc = check_ctx(c);
+    if (rc != MSIM_OK) return rc;
+    if (flags & ~MSIM_STEP_NEIGHBOURS) return fail(MSIM_ERR_INVALID, "unknown step flags");
+    if (c->n == 0) {
+        c->tick += ticks;
+        return MSIM_OK;
+    }
+    if (flags & MSIM_STEP_NEIGHBOURS) {
+        for (uint32_t t = 0; t < ticks; t++) {
+            rc = neighbour_tick(c);
+            if (rc != MSIM_OK) return rc;
+            c->tick++;
+        }
+        return MSIM_OK;
+    }
+    // move only: up to 256 ticks per launch with the state in registers
+    uint32_t left = ticks;
+    while (left) {
+        uint32_t t = std::min<uint32_t>(left, 256u);
+        Prof p(c, K_STEP_MULTI);
+        CK(launch_step(c->stream, step_args(c, t, false)), "k_step_multi");
+        left -= t;
+        c->tick += t;
+    }
+    return MSIM_OK;
+}
+
+int msim_sync(msim_ctx* c) {
+    int rc = check_ctx(c);
+    if (rc != MSIM_OK) return rc;
+    return sync_and_check(c);
+}
+
+int msim_get_state(msim_ctx* c, float* pos, uint32_t* heading, uint32_t* rng, float* speed) {
+    int rc = check_ctx(c);
+    if (rc != MSIM_OK) return rc;
+    const size_t n = c->n;
+    if (n == 0) return sync_and_check(c);
+    if ((rc = ensure_stage(c, n * (sizeof(float2) + sizeof(uint32_t) + sizeof(uint4) + sizeof(float)))) != MSIM_OK)
+        return rc;
+    char* b = static_cast<char*>(c->stage);
+    uint4* d_rng = reinterpret_cast<uint4*>(b);
+    float2* d_pos = reinterpret_cast<float2*>(b + n * sizeof(uint4));
+    uint32_t* d_head = reinterpret_cast<uint32_t*>(b + n * (sizeof(uint4) + sizeof(float2)));
+    float* d_speed = reinterpret_cast<float*>(b + n * (sizeof(uint4) + sizeof(float2) + sizeof(uint32_t)));
+    {
+        Prof p(c, K_EXPORT);
+        CK(launch_export_state(c->stream, cur_state(c), c->n, pos ? d_pos : nullptr, heading ? d_head : nullptr,
+                               rng ? d_rng : nullptr, speed ? d_speed : nullptr),
+           "k_export_state");
+    }
+    if (pos) CK(cudaMemcpyAsync(pos, d_pos, sizeof(float2) * n, cudaMemcpyDeviceToHost, c->stream), "download pos");
+    if (heading)
+        CK(cudaMemcpyAsync(heading, d_head, sizeof(uint32_t) * n, cudaMemcpyDeviceToHost, c->stream), "download heading");
+    if (rng) CK(cudaMemcpyAsync(rng, d_rng, sizeof(uint4) * n, cudaMemcpyDeviceToHost, c->stream), "download rng");
+    if (speed) CK(cudaMemcpyAsync(speed, d_speed, sizeof(float) * n, cudaMemcpyDeviceToHost, c->stream), "download speed");
+    return sync_and_check(c);
+}
+
+int msim_get_neighbours(msim_ctx* c, uint32_t* count, uint32_t* idx) {
+    int rc = check_ctx(c);
+    if (rc != MSIM_OK) return rc;
+    if (!count) return fail(MSIM_ERR_INVALID, "count is NULL");
+    if (!c->have_nbr) return fail(MSIM_ERR_INVALID, "no neighbour tick has run since the entities were set");
+    const size_t n = c->n, cap = c->params.cap;
+    if (n == 0) return MSIM_OK;
+    const bool want_idx = idx && cap;
+    if ((rc = ensure_stage(c, n * sizeof(uint32_t) * (1 + (want_idx ? cap : 0)))) != MSIM_OK) return rc;
+    uint32_t* d_count = static_cast<uint32_t*>(c->stage);
+    uint32_t* d_idx = want_idx ? d_count + n : nullptr;
+    {
+        Prof p(c, K_EXPORT);
+        CK(launch_export_neighbours(c->stream, c->sorted_slot, cur_state(c).slot_id, c->nbr_count, c->nbr_list,
+                                    c->n, c->params.cap, d_count, d_idx),
+           "k_export_nbr");
+    }
+    CK(cudaMemcpyAsync(count, d_count, sizeof(uint32_t) * n, cudaMemcpyDeviceToHost, c->stream), "download counts");
+    if (want_idx)
+        CK(cudaMemcpyAsync(idx, d_idx, sizeof(uint32_t) * n * cap, cudaMemcpyDeviceToHost, c->stream),
+           "download neighbours");
+    return sync_and_check(c);
+}
+
+int msim_get_collision_pairs(msim_ctx* c, uint64_t* pairs) {
+    int rc = check_ctx(c);
+    if (rc != MSIM_OK) return rc;
+    if (!pairs) return fail(MSIM_ERR_INVALID, "pairs is NULL");
+    if (!c->have_nbr) return fail(MSIM_ERR_INVALID, "no neighbour tick has run since the entities were set");
+    unsigned long long h = 0;
+    CK(cudaMemcpyAsync(&h, c->pairs, sizeof(h), cudaMemcpyDeviceToHost, c->stream), "download pairs");
+    rc = sync_and_check(c);
+    *pairs = h;
+    return rc;
+}
+
+int msim_export_entities_aos(msim_ctx* c, void* out, size_t n) {
+    int rc = check_ctx(c);
+    if (rc != MSIM_OK) return rc;
+    if (!out && n) return fail(MSIM_ERR_INVALID, "out is NULL");
+    if (n != c->n) return fail(MSIM_ERR_INVALID, "n must equal num_entities");
+    if (n == 0) return MSIM_OK;
+    if ((rc = ensure_stage(c, n * 64)) != MSIM_OK) return rc;
+    {
+        Prof p(c, K_EXPORT);
+        CK(launch_export_aos(c->stream, c->dmap(), cur_state(c), c->n, c->params.dt,
+                             c->have_nbr ? c->sorted_slot : nullptr, c->have_nbr ? c->nbr_count : nullptr, c->stage),
+           "k_export_aos");
+    }
+    CK(cudaMemcpyAsync(out, c->stage, n * 64, cudaMemcpyDeviceToHost, c->stream), "download entities");
+    return sync_and_check(c);
+}
+
+int msim_get_tick(msim_ctx* c, uint64_t* tick) {
+    if (!c || !tick) return fail(MSIM_ERR_INVALID, "NULL argument");
+    *tick = c->tick;
+    return MSIM_OK;
+}
+
+int msim_set_profiling(msim_ctx* c, int enable) {
+    int rc = check_ctx(c);
+    if (rc != MSIM_OK) return rc;
+    c->profiling = enable != 0;
+    return MSIM_OK;
+}
+
+int msim_reset_kernel_stats(msim_ctx* c) {
+    int rc = check_ctx(c);
+    if (rc != MSIM_OK) return rc;
+    rc = drain_profile(c);
+    for (uint32_t k = 0; k < K_COUNT; k++) {
+        c->launches[k] = 0;
+        c->ms[k] = 0.0;
+    }
+    return rc;
+}
+
+int msim_get_kernel_stats(msim_ctx* c, uint32_t kernel, uint64_t* launches, double* total_ms) {
+    int rc = check_ctx(c);
+    if (rc != MSIM_OK) return rc;
+    if (kernel >= K_COUNT) return fail(MSIM_ERR_INVALID, "unknown kernel id");
+    rc = drain_profile(c);
+    if (rc != MSIM_OK) return rc;
+    if (launches) *launches = c->launches[kernel];
+    if (total_ms) *total_ms = c->ms[kernel];
+    return MSIM_OK;
+}
+
+int msim_timer_begin(msim_ctx* c) {
+    int rc = check_ctx(c);
+    if (rc != MSIM_OK) return rc;
+    CK(cudaEventRecord(c->t0, c->stream), "cudaEventRecord");
+    c->timer_open = true;
+    return MSIM_OK;
+}
+
+int msim_timer_end(msim_ctx* c, float* ms) {
+    int rc = check_ctx(c);
+    if (rc != MSIM_OK) return rc;
+    if (!c->timer_open || !ms) return fail(MSIM_ERR_INVALID, "timer not started or ms is NULL");
+    CK(cudaEventRecord(c->t1, c->stream), "cudaEventRecord");
+    CK(cudaEventSynchronize(c->t1), "cudaEventSynchronize");
+    CK(cudaEventElapsedTime(ms, c->t0, c->t1), "cudaEventElapsedTime");
+    c->timer_open = false;
+    return MSIM_OK;
+}
+
+int msim_host_alloc(size_t bytes, void** out) {
+    if (!out) return fail(MSIM_ERR_INVALID, "out is NULL");
+    *out = nullptr;
+    cudaError_t e = cudaMallocHost(out, bytes ? bytes : 1);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return fail(MSIM_ERR_NOMEM, std::string("cudaMallocHost failed: ") + cudaGetErrorString(e));
+    }
+    return MSIM_OK;
+}
+
+int msim_host_free(void* ptr) {
+    if (!ptr) return MSIM_OK;
+    cudaError_t e = cudaFreeHost(ptr);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaFreeHost");
+    return MSIM_OK;
+}
+
+int msim_get_info(msim_ctx* c, msim_info* out) {
+    if (!c || !out) return fail(MSIM_ERR_INVALID, "NULL argument");
+    out->num_entities = c->n;
+    out->num_roads = c->R;
+    out->num_connections = c->C;
+    out->tiles_x = c->grid.tiles_x;
+    out->tiles_y = c->grid.tiles_y;
+    out->key_bits = 2 * c->grid.bits;
+    out->sort_passes = c->passes;
+    out->resort_interval = c->resort;
+    out->cell_size = 1.f / c->grid.inv_cell;
+    out->cap = c->params.cap;
+    out->device_bytes = c->device_bytes;
+    return MSIM_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,577 @@
+// CUDA kernels of the movement-sim per-tick path for sm_103a.
+//
+// Per neighbour tick (entity state is kept in "slot" order, i.e. the spatial
+// order of the last re-ordering):
+//   k_step      move every entity one tick (random_move.comp:869-874), write its
+//               tile Morton key and count the key's radix digits (warp-aggregated
+//               with __match_any_sync, one shared atomic per digit group)
+//   k_hist_scan exclusive offsets of each digit pass
+//   k_onesweep  one stable LSD radix pass per 8-bit digit (decoupled look-back,
+//               warp-level multi-split ranking with __match_any_sync)
+//   k_ranges    [start, end) of each occupied tile in the sorted order
+//   k_query     radius neighbour query (random_move.comp:541-719 semantics: the
+//               pair predicate of :551-562), count + the cap smallest ids
+// Every few ticks k_permute re-orders the entity state by the sorted order so
+// that the step and the query keep reading memory almost sequentially.
+#include <cstdio>
+
+#include "msim_kernels.cuh"
+
+namespace msim {
+namespace {
+
+constexpr uint32_t kFlagAgg = 0x40000000u;
+constexpr uint32_t kFlagPrefix = 0x80000000u;
+constexpr uint32_t kFlagMask = 0xc0000000u;
+constexpr uint32_t kValueMask = 0x3fffffffu;
+constexpr uint32_t kSpinLimit = 1u << 24;  // ~1 s of polling, then give up with kErrTimeout
+
+__device__ __forceinline__ uint32_t lanemask_lt() {
+    uint32_t m;
+    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+    return m;
+}
+__device__ __forceinline__ uint32_t ld_relaxed(const uint32_t* p) {
+    uint32_t v;
+    asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void st_relaxed(uint32_t* p, uint32_t v) {
+    asm volatile("st.relaxed.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// Block-wide exclusive sum over NT threads; s_warp needs NT/32 + 1 words.
+// All threads must call it; returns the exclusive prefix, *total = block sum.
+template <int NT>
+__device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t* s_warp, uint32_t* total) {
+    constexpr int NW = NT / 32;
+    const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint32_t x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= (uint32_t)o) x += y;
+    }
+    if (lane == 31) s_warp[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+        uint32_t w = lane < (uint32_t)NW ? s_warp[lane] : 0u;
+        uint32_t incl = w;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= (uint32_t)o) incl += y;
+        }
+        if (lane < (uint32_t)NW) s_warp[lane] = incl - w;
+        if (lane == (uint32_t)NW - 1) s_warp[NW] = incl;
+    }
+    __syncthreads();
+    uint32_t r = s_warp[warp] + x - v;
+    if (total) *total = s_warp[NW];
+    __syncthreads();
+    return r;
+}
+
+__device__ __forceinline__ uint4 pcg32_seed(uint64_t initstate, uint64_t initseq) {
+    uint64_t inc = (initseq << 1) | 1u;
+    uint4 s = make_uint4(0u, 0u, (uint32_t)inc, (uint32_t)(inc >> 32));
+    (void)pcg32_next(s);
+    uint64_t st = (((uint64_t)s.y << 32) | s.x) + initstate;
+    s.x = (uint32_t)st;
+    s.y = (uint32_t)(st >> 32);
+    (void)pcg32_next(s);
+    return s;
+}
+
+// Deterministic initializer (replaces Simulator.cpp:114-129, Entity.cpp:44-49):
+// draw streams 1 road, 2 fraction along the road, 3 speed, 4/5 RNG state.
+__global__ void k_init(DeviceMap m, EntityState st, uint32_t n, uint32_t rng_kind, uint64_t seed,
+                       uint32_t placement, float smin, float smax) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        uint64_t dr = d_draw(seed, 1, i);
+        uint32_t r = (uint32_t)(((dr >> 32) * (uint64_t)m.num_roads) >> 32);
+        float4 rp = m.road_pos[r];
+        float px = rp.x, py = rp.y;
+        if (placement == 1) {
+            float u = unit24(d_draw(seed, 2, i));
+            px = __fadd_rn(rp.x, __fmul_rn(u, __fsub_rn(rp.z, rp.x)));
+            py = __fadd_rn(rp.y, __fmul_rn(u, __fsub_rn(rp.w, rp.y)));
+        }
+        st.pos[i] = make_float2(px, py);
+        st.head[i] = r | kHeadToEnd;
+        float v = unit24(d_draw(seed, 3, i));
+        st.speed[i] = __fadd_rn(smin, __fmul_rn(v, __fsub_rn(smax, smin)));
+        uint64_t a = d_draw(seed, 4, i);
+        uint64_t b = d_draw(seed, 5, i);
+        uint4 s;
+        if (rng_kind == 1) {
+            s = pcg32_seed(a, b);
+        } else {
+            s = make_uint4((uint32_t)a, (uint32_t)(a >> 32), (uint32_t)b, (uint32_t)(b >> 32));
+            if ((s.x | s.y | s.z | s.w) == 0u) s.x = 1u;
+        }
+        st.rng[i] = s;
+        st.slot_id[i] = i;
+    }
+}
+
+// Move `ticks` ticks (state kept in registers across ticks), then optionally
+// write the tile key and accumulate the radix digit histograms of all passes.
+template <int RNG, bool KEY>
+__global__ __launch_bounds__(kStepThreads) void k_step(StepLaunch a) {
+    __shared__ uint32_t s_hist[kMaxPasses * kRadix];
+    if (KEY) {
+        for (uint32_t i = threadIdx.x; i < a.passes * kRadix; i += kStepThreads) s_hist[i] = 0u;
+        __syncthreads();
+    }
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t stride = gridDim.x * kStepThreads;
+    for (uint32_t base = blockIdx.x * kStepThreads; base < a.n; base += stride) {
+        const uint32_t s = base + threadIdx.x;
+        const bool valid = s < a.n;
+        uint32_t key = 0u;
+        if (valid) {
+            float2 p = a.st.pos[s];
+            if (a.ticks) {
+                uint32_t h = a.st.head[s];
+                const uint32_t h0 = h;
+                const float sp = a.st.speed[s];
+                uint4 r = make_uint4(0u, 0u, 0u, 0u);
+                bool rl = false, rd = false;
+                for (uint32_t t = 0; t < a.ticks; t++)
+                    step_entity<RNG>(a.map, a.dt, sp, p, h, r, rl, rd, a.st.rng + s, a.err);
+                a.st.pos[s] = p;
+                if (h != h0) a.st.head[s] = h;
+                if (rd) a.st.rng[s] = r;
+            }
+            if (KEY) {
+                key = tile_key(a.grid, p);
+                a.key[s] = key;
+            }
+        }
+        if (KEY) {
+            const unsigned vm = __ballot_sync(0xffffffffu, valid);
+            if (valid) {
+                for (uint32_t ps = 0; ps < a.passes; ps++) {
+                    const uint32_t d = (key >> (8u * ps)) & 0xffu;
+                    const unsigned peers = __match_any_sync(vm, d);
+                    if ((int)lane == __ffs(peers) - 1) atomicAdd(&s_hist[ps * kRadix + d], (uint32_t)__popc(peers));
+                }
+            }
+        }
+    }
+    if (KEY) {
+        __syncthreads();
+        for (uint32_t i = threadIdx.x; i < a.passes * kRadix; i += kStepThreads) {
+            const uint32_t c = s_hist[i];
+            if (c) atomicAdd(&a.hist[i], c);
+        }
+    }
+}
+
+__global__ __launch_bounds__(kRadix) void k_hist_scan(const uint32_t* hist, uint32_t* off, uint32_t passes) {
+    __shared__ uint32_t s_warp[kRadix / 32 + 1];
+    for (uint32_t ps = 0; ps < passes; ps++) {
+        uint32_t v = hist[ps * kRadix + threadIdx.x];
+        off[ps * kRadix + threadIdx.x] = block_exclusive_scan<kRadix>(v, s_warp, nullptr);
+    }
+}
+
+// One stable LSD radix pass over 8 bits of the key (Adinets & Merrill,
+// "Onesweep", 2022).  Blocks take tiles in launch order through an atomic ticket,
+// rank their 4096 items with warp-level multi-split (__match_any_sync) into
+// per-warp digit counters, publish per-digit counts and resolve their global
+// offsets by looking back over earlier tiles.  Every wait is bounded.
+__global__ __launch_bounds__(kSortThreads) void k_onesweep(const uint32_t* __restrict__ keys_in,
+                                                           const uint32_t* __restrict__ vals_in,
+                                                           uint32_t* __restrict__ keys_out,
+                                                           uint32_t* __restrict__ vals_out, uint32_t n,
+                                                           uint32_t shift, const uint32_t* __restrict__ digit_offset,
+                                                           uint32_t* lookback, uint32_t* ticket, uint32_t* err) {
+    constexpr int NW = kSortThreads / 32;
+    __shared__ uint32_t s_keys[kSortTile];
+    __shared__ uint32_t s_vals[kSortTile];
+    __shared__ uint32_t s_whist[NW * kRadix];  // per-warp counts, then exclusive warp prefix
+    __shared__ uint32_t s_local_start[kRadix];
+    __shared__ uint32_t s_global_base[kRadix];
+    __shared__ uint32_t s_warp[NW + 1];
+    __shared__ uint32_t s_tile;
+
+    const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    if (tid == 0) s_tile = atomicAdd(ticket, 1u);
+    for (uint32_t i = tid; i < NW * kRadix; i += kSortThreads) s_whist[i] = 0u;
+    __syncthreads();
+    const uint32_t tile = s_tile;
+    const uint32_t base = tile * kSortTile;
+
+    uint32_t k[kSortRows], v[kSortRows], rk[kSortRows];
+#pragma unroll
+    for (int r = 0; r < kSortRows; r++) {
+        const uint32_t idx = base + warp * (kSortRows * 32) + r * 32 + lane;
+        const bool ok = idx < n;
+        k[r] = ok ? keys_in[idx] : 0u;
+        v[r] = ok ? (vals_in ? vals_in[idx] : idx) : 0u;
+        rk[r] = 0u;
+    }
+    // warp-level multi-split ranking, rows in order -> stable
+    uint32_t* wh = s_whist + warp * kRadix;
+    const uint32_t lt = lanemask_lt();
+#pragma unroll
+    for (int r = 0; r < kSortRows; r++) {
+        const uint32_t idx = base + warp * (kSortRows * 32) + r * 32 + lane;
+        const bool ok = idx < n;
+        const unsigned vm = __ballot_sync(0xffffffffu, ok);
+        if (ok) {
+            const uint32_t d = (k[r] >> shift) & 0xffu;
+            const unsigned peers = __match_any_sync(vm, d);
+            const uint32_t cnt = wh[d];
+            rk[r] = cnt + (uint32_t)__popc(peers & lt);
+            __syncwarp(vm);
+            if ((int)lane == __ffs(peers) - 1) wh[d] = cnt + (uint32_t)__popc(peers);
+        }
+        __syncwarp();
+    }
+    __syncthreads();
+
+    // one thread per digit: warp prefix, block count, publication, look-back
+    const uint32_t d = tid;
+    uint32_t tot = 0u;
+#pragma unroll
+    for (int w = 0; w < NW; w++) {
+        const uint32_t c = s_whist[w * kRadix + d];
+        s_whist[w * kRadix + d] = tot;
+        tot += c;
+    }
+    uint32_t* my_lb = lookback + (size_t)tile * kRadix + d;
+    st_relaxed(my_lb, (tile == 0 ? kFlagPrefix : kFlagAgg) | tot);
+    uint32_t excl = 0u;
+    if (tile > 0) {
+        int32_t j = (int32_t)tile - 1;
+        uint32_t spins = 0u;
+        while (j >= 0) {
+            const uint32_t w = ld_relaxed(lookback + (size_t)j * kRadix + d);
+            if ((w & kFlagMask) == 0u) {
+                if (++spins > kSpinLimit) {
+                    atomicOr(err, kErrTimeout);
+                    break;
+                }
+                __nanosleep(32);
+                continue;
+            }
+            excl += w & kValueMask;
+            if (w & kFlagPrefix) break;
+            j--;
+        }
+        st_relaxed(my_lb, kFlagPrefix | ((excl + tot) & kValueMask));
+    }
+    s_global_base[d] = digit_offset[d] + excl;
+    s_local_start[d] = block_exclusive_scan<kSortThreads>(tot, s_warp, nullptr);
+
+    // local scatter into shared memory (digit-major), then coalesced runs out
+#pragma unroll
+    for (int r = 0; r < kSortRows; r++) {
+        const uint32_t idx = base + warp * (kSortRows * 32) + r * 32 + lane;
+        if (idx < n) {
+            const uint32_t dd = (k[r] >> shift) & 0xffu;
+            const uint32_t lpos = s_local_start[dd] + s_whist[warp * kRadix + dd] + rk[r];
+            s_keys[lpos] = k[r];
+            s_vals[lpos] = v[r];
+        }
+    }
+    __syncthreads();
+    const uint32_t count = (n - base) < kSortTile ? (n - base) : kSortTile;
+    for (uint32_t i = tid; i < count; i += kSortThreads) {
+        const uint32_t key = s_keys[i];
+        const uint32_t dd = (key >> shift) & 0xffu;
+        const uint32_t g = s_global_base[dd] + (i - s_local_start[dd]);
+        keys_out[g] = key;
+        vals_out[g] = s_vals[i];
+    }
+}
+
+__global__ void k_ranges(const uint32_t* __restrict__ sk, uint32_t n, uint32_t* __restrict__ ranges) {
+    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n) return;
+    const uint32_t k = sk[p];
+    if (p == 0 || sk[p - 1] != k) ranges[2ull * k] = p;
+    if (p + 1 == n || sk[p + 1] != k) ranges[2ull * k + 1] = p + 1;
+}
+
+// Neighbour query, one thread per sorted position.  Candidates come from every
+// tile overlapping [pos - reach, pos + reach]; the kept list is the cap smallest
+// entity ids in ascending order, built by insertion into a per-thread column of
+// shared memory (column-interleaved: no bank conflicts).  Each block writes its
+// lists contiguously at block * kQueryThreads * cap.
+template <bool LIST>
+__global__ __launch_bounds__(kQueryThreads) void k_query(const uint32_t* __restrict__ sorted_slot,
+                                                         const float2* __restrict__ pos,
+                                                         const uint32_t* __restrict__ slot_id,
+                                                         const uint2* __restrict__ ranges, TileGrid g,
+                                                         uint32_t n, uint32_t cap, uint32_t* __restrict__ count_out,
+                                                         uint32_t* __restrict__ list, unsigned long long* pairs) {
+    extern __shared__ uint32_t s_list[];
+    __shared__ uint32_t s_warp[kQueryThreads / 32 + 1];
+    const uint32_t tid = threadIdx.x;
+    const uint32_t p = blockIdx.x * kQueryThreads + tid;
+    uint32_t count = 0u, lower = 0u;
+    if (p < n) {
+        const uint32_t s = sorted_slot[p];
+        const float2 me = pos[s];
+        const uint32_t myid = slot_id[s];
+        const uint32_t x0 = tile_coord(__fsub_rn(me.x, g.reach), g.inv_cell, g.tiles_x);
+        const uint32_t x1 = tile_coord(__fadd_rn(me.x, g.reach), g.inv_cell, g.tiles_x);
+        const uint32_t y0 = tile_coord(__fsub_rn(me.y, g.reach), g.inv_cell, g.tiles_y);
+        const uint32_t y1 = tile_coord(__fadd_rn(me.y, g.reach), g.inv_cell, g.tiles_y);
+        for (uint32_t ty = y0; ty <= y1; ty++) {
+            for (uint32_t tx = x0; tx <= x1; tx++) {
+                const uint2 rg = ranges[morton2(tx, ty)];
+                for (uint32_t q = rg.x; q < rg.y; q++) {
+                    const uint32_t s2 = sorted_slot[q];
+                    if (s2 == s) continue;
+                    if (!in_range(pos[s2], me, g.radius)) continue;
+                    const uint32_t oid = slot_id[s2];
+                    lower += oid < myid ? 1u : 0u;
+                    if (LIST) {
+                        const uint32_t m = count < cap ? count : cap;
+                        if (m < cap || oid < s_list[(cap - 1) * kQueryThreads + tid]) {
+                            uint32_t j = m < cap ? m : cap - 1;
+                            while (j > 0) {
+                                const uint32_t prev = s_list[(j - 1) * kQueryThreads + tid];
+                                if (prev <= oid) break;
+                                s_list[j * kQueryThreads + tid] = prev;
+                                j--;
+                            }
+                            s_list[j * kQueryThreads + tid] = oid;
+                        }
+                    }
+                    count++;
+                }
+            }
+        }
+        count_out[p] = count;
+    }
+    uint32_t block_lower = 0u;
+    (void)block_exclusive_scan<kQueryThreads>(lower, s_warp, &block_lower);
+    if (tid == 0 && block_lower) atomicAdd(pairs, (unsigned long long)block_lower);
+    if (LIST) {
+        const uint32_t kept = count < cap ? count : cap;
+        const uint32_t off = block_exclusive_scan<kQueryThreads>(kept, s_warp, nullptr);
+        uint32_t* out = list + (size_t)blockIdx.x * kQueryThreads * cap + off;
+        for (uint32_t j = 0; j < kept; j++) out[j] = s_list[j * kQueryThreads + tid];
+    }
+}
+
+__global__ void k_permute(const uint32_t* __restrict__ ss, EntityState src, EntityState dst, uint32_t n) {
+    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n) return;
+    const uint32_t s = ss[p];
+    dst.pos[p] = src.pos[s];
+    dst.head[p] = src.head[s];
+    dst.rng[p] = src.rng[s];
+    dst.speed[p] = src.speed[s];
+    dst.slot_id[p] = src.slot_id[s];
+}
+
+__global__ void k_export_state(EntityState st, uint32_t n, float2* pos, uint32_t* head, uint4* rng, float* speed) {
+    const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n) return;
+    const uint32_t id = st.slot_id[s];
+    if (id >= n) return;
+    if (pos) pos[id] = st.pos[s];
+    if (head) head[id] = st.head[s];
+    if (rng) rng[id] = st.rng[s];
+    if (speed) speed[id] = st.speed[s];
+}
+
+__global__ __launch_bounds__(kQueryThreads) void k_export_nbr(const uint32_t* sorted_slot, const uint32_t* slot_id,
+                                                              const uint32_t* count, const uint32_t* list,
+                                                              uint32_t n, uint32_t cap, uint32_t* out_count,
+                                                              uint32_t* out_idx) {
+    __shared__ uint32_t s_warp[kQueryThreads / 32 + 1];
+    const uint32_t p = blockIdx.x * kQueryThreads + threadIdx.x;
+    const uint32_t c = p < n ? count[p] : 0u;
+    const uint32_t kept = c < cap ? c : cap;
+    const uint32_t off = block_exclusive_scan<kQueryThreads>(kept, s_warp, nullptr);
+    if (p >= n) return;
+    const uint32_t s = sorted_slot ? sorted_slot[p] : p;
+    const uint32_t id = slot_id[s];
+    if (id >= n) return;
+    out_count[id] = c;
+    if (out_idx && cap) {
+        const uint32_t* src = list + (size_t)blockIdx.x * kQueryThreads * cap + off;
+        uint32_t* dst = out_idx + (size_t)id * cap;
+        for (uint32_t j = 0; j < cap; j++) dst[j] = j < kept ? src[j] : 0xffffffffu;
+    }
+}
+
+// Entity.hpp:33-46 record: color, randomState, pos, target, direction, roadIndex,
+// initialized.  direction = update_direction(pos) (random_move.comp:830-839).
+__global__ void k_export_aos(DeviceMap m, EntityState st, uint32_t n, float dt, uint4* out) {
+    const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n) return;
+    const uint32_t id = st.slot_id[s];
+    if (id >= n) return;
+    const float2 p = st.pos[s];
+    const uint32_t h = st.head[s];
+    const uint32_t road = h & kHeadRoad;
+    float tx = p.x, ty = p.y, f = 1.f;
+    if (road < m.num_roads) {
+        const float4 rp = m.road_pos[road];
+        tx = (h & kHeadToEnd) ? rp.z : rp.x;
+        ty = (h & kHeadToEnd) ? rp.w : rp.y;
+        if (m.factor) f = m.factor[road];
+    }
+    const float step = __fmul_rn(__fmul_rn(st.speed[s], f), dt);
+    const float dx = __fsub_rn(tx, p.x), dy = __fsub_rn(ty, p.y);
+    const float len = __fsqrt_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)));
+    float dirx = 0.f, diry = 0.f;
+    if (len != 0.f) {
+        dirx = __fmul_rn(__fdiv_rn(dx, len), step);
+        diry = __fmul_rn(__fdiv_rn(dy, len), step);
+    }
+    uint4* rec = out + (size_t)id * 4;
+    rec[0] = make_uint4(__float_as_uint(1.f), 0u, 0u, __float_as_uint(1.f));  // red until a collision tick
+    rec[1] = st.rng[s];
+    rec[2] = make_uint4(__float_as_uint(p.x), __float_as_uint(p.y), __float_as_uint(tx), __float_as_uint(ty));
+    rec[3] = make_uint4(__float_as_uint(dirx), __float_as_uint(diry), road, 1u);
+}
+
+// collision colours of the last neighbour tick (random_move.comp:545-549, 876)
+__global__ void k_export_colors(const uint32_t* sorted_slot, const uint32_t* slot_id, const uint32_t* count,
+                                 uint32_t n, uint4* out) {
+    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n) return;
+    const uint32_t s = sorted_slot ? sorted_slot[p] : p;
+    const uint32_t id = slot_id[s];
+    if (id >= n) return;
+    const bool hit = count[p] > 0u;
+    out[(size_t)id * 4] = make_uint4(0u, hit ? 0u : __float_as_uint(1.f), hit ? __float_as_uint(1.f) : 0u,
+                                     __float_as_uint(1.f));
+}
+
+__global__ void k_iota(uint32_t* out, uint32_t n) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] = i;
+}
+
+inline unsigned blocks_for(uint32_t n, unsigned threads) { return (unsigned)((n + threads - 1) / threads); }
+
+}  // namespace
+
+int query_smem_bytes(uint32_t cap) { return (int)(cap * kQueryThreads * sizeof(uint32_t)); }
+
+cudaError_t configure_kernels(uint32_t cap) {
+    int bytes = query_smem_bytes(cap);
+    if (bytes > 48 * 1024) {
+        cudaError_t e = cudaFuncSetAttribute(k_query<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+}
+
+int step_blocks_for(int device, uint32_t n) {
+    int sms = 0, per_sm = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_step<0, true>, kStepThreads, 0);
+    if (sms <= 0) sms = 1;
+    if (per_sm <= 0) per_sm = 1;
+    long long want = (long long)sms * per_sm;
+    long long need = (n + kStepThreads - 1) / kStepThreads;
+    if (need < 1) need = 1;
+    return (int)(want < need ? want : need);
+}
+
+cudaError_t launch_init_entities(cudaStream_t s, const DeviceMap& m, EntityState st, uint32_t n, uint32_t rng_kind,
+                                 uint64_t seed, uint32_t placement, float smin, float smax) {
+    if (n == 0) return cudaSuccess;
+    unsigned blocks = blocks_for(n, 256);
+    if (blocks > 65535u * 8u) blocks = 65535u * 8u;
+    k_init<<<blocks, 256, 0, s>>>(m, st, n, rng_kind, seed, placement, smin, smax);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_step(cudaStream_t s, const StepLaunch& a) {
+    if (a.n == 0) return cudaSuccess;
+    const bool key = a.key != nullptr;
+    if (a.rng_kind == 1) {
+        if (key) k_step<1, true><<<a.blocks, kStepThreads, 0, s>>>(a);
+        else k_step<1, false><<<a.blocks, kStepThreads, 0, s>>>(a);
+    } else {
+        if (key) k_step<0, true><<<a.blocks, kStepThreads, 0, s>>>(a);
+        else k_step<0, false><<<a.blocks, kStepThreads, 0, s>>>(a);
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_hist_scan(cudaStream_t s, const uint32_t* hist, uint32_t* offsets, uint32_t passes) {
+    k_hist_scan<<<1, kRadix, 0, s>>>(hist, offsets, passes);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_onesweep(cudaStream_t s, const uint32_t* keys_in, const uint32_t* vals_in, uint32_t* keys_out,
+                            uint32_t* vals_out, uint32_t n, uint32_t shift, const uint32_t* digit_offset,
+                            uint32_t* lookback, uint32_t* ticket, uint32_t* err) {
+    if (n == 0) return cudaSuccess;
+    k_onesweep<<<blocks_for(n, kSortTile), kSortThreads, 0, s>>>(keys_in, vals_in, keys_out, vals_out, n, shift,
+                                                                 digit_offset, lookback, ticket, err);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_ranges(cudaStream_t s, const uint32_t* sorted_key, uint32_t n, uint2* ranges) {
+    if (n == 0) return cudaSuccess;
+    k_ranges<<<blocks_for(n, 256), 256, 0, s>>>(sorted_key, n, reinterpret_cast<uint32_t*>(ranges));
+    return cudaGetLastError();
+}
+
+cudaError_t launch_query(cudaStream_t s, uint32_t cap, const uint32_t* sorted_slot, const float2* pos,
+                         const uint32_t* slot_id, const uint2* ranges, TileGrid grid, uint32_t n, uint32_t* count,
+                         uint32_t* list, unsigned long long* pairs) {
+    if (n == 0) return cudaSuccess;
+    if (cap > 0 && list)
+        k_query<true><<<blocks_for(n, kQueryThreads), kQueryThreads, query_smem_bytes(cap), s>>>(
+            sorted_slot, pos, slot_id, ranges, grid, n, cap, count, list, pairs);
+    else
+        k_query<false><<<blocks_for(n, kQueryThreads), kQueryThreads, 0, s>>>(sorted_slot, pos, slot_id, ranges,
+                                                                             grid, n, 0u, count, nullptr, pairs);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_iota(cudaStream_t s, uint32_t* out, uint32_t n) {
+    if (n == 0) return cudaSuccess;
+    k_iota<<<blocks_for(n, 256), 256, 0, s>>>(out, n);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_permute(cudaStream_t s, const uint32_t* sorted_slot, EntityState src, EntityState dst, uint32_t n) {
+    if (n == 0) return cudaSuccess;
+    k_permute<<<blocks_for(n, 256), 256, 0, s>>>(sorted_slot, src, dst, n);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_export_state(cudaStream_t s, EntityState st, uint32_t n, float2* pos, uint32_t* head, uint4* rng,
+                                float* speed) {
+    if (n == 0) return cudaSuccess;
+    k_export_state<<<blocks_for(n, 256), 256, 0, s>>>(st, n, pos, head, rng, speed);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_export_neighbours(cudaStream_t s, const uint32_t* sorted_slot, const uint32_t* slot_id,
+                                     const uint32_t* count, const uint32_t* list, uint32_t n, uint32_t cap,
+                                     uint32_t* out_count, uint32_t* out_idx) {
+    if (n == 0) return cudaSuccess;
+    k_export_nbr<<<blocks_for(n, kQueryThreads), kQueryThreads, 0, s>>>(sorted_slot, slot_id, count, list, n, cap,
+                                                                        out_count, out_idx);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_export_aos(cudaStream_t s, const DeviceMap& m, EntityState st, uint32_t n, float dt,
+                              const uint32_t* sorted_slot, const uint32_t* count, void* out) {
+    if (n == 0) return cudaSuccess;
+    k_export_aos<<<blocks_for(n, 256), 256, 0, s>>>(m, st, n, dt, static_cast<uint4*>(out));
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess || !count) return e;
+    k_export_colors<<<blocks_for(n, 256), 256, 0, s>>>(sorted_slot, st.slot_id, count, n, static_cast<uint4*>(out));
+    return cudaGetLastError();
+}
+
+}  // namespace msim

@@ -1,0 +1,73 @@
+// Kernel launchers of the movement-sim per-tick path (implemented in msim_kernels.cu).
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "msim_device.cuh"
+
+namespace msim {
+
+// Radix sort (onesweep: one global histogram pass, then one chained-scan pass per digit)
+constexpr int kSortThreads = 256;
+constexpr int kSortRows = 16;                               // items per thread
+constexpr uint32_t kSortTile = kSortThreads * kSortRows;    // 4096 items per block
+constexpr uint32_t kRadix = 256;                            // 8-bit digits
+constexpr int kMaxPasses = 3;                               // keys up to 24 bits
+constexpr int kQueryThreads = 128;
+constexpr int kStepThreads = 256;
+constexpr uint32_t kMaxCap = 256;
+
+// Entity state in slot order (structure of arrays)
+struct EntityState {
+    float2* pos;
+    uint32_t* head;
+    uint4* rng;
+    float* speed;
+    uint32_t* slot_id;  // entity id held by each slot
+};
+
+struct StepLaunch {
+    DeviceMap map;
+    EntityState st;
+    uint32_t n;
+    float dt;
+    uint32_t ticks;       // 0: only keys/histogram of the current positions
+    uint32_t rng_kind;
+    uint32_t* key;        // nullptr: no spatial key
+    uint32_t* hist;       // passes * 256 digit counts (accumulated)
+    TileGrid grid;
+    uint32_t passes;
+    uint32_t* err;
+    int blocks;           // grid size (grid-stride loop)
+};
+
+cudaError_t launch_init_entities(cudaStream_t s, const DeviceMap& m, EntityState st, uint32_t n,
+                                 uint32_t rng_kind, uint64_t seed, uint32_t placement, float smin,
+                                 float smax);
+cudaError_t launch_step(cudaStream_t s, const StepLaunch& a);
+cudaError_t launch_hist_scan(cudaStream_t s, const uint32_t* hist, uint32_t* offsets, uint32_t passes);
+cudaError_t launch_onesweep(cudaStream_t s, const uint32_t* keys_in, const uint32_t* vals_in,
+                            uint32_t* keys_out, uint32_t* vals_out, uint32_t n, uint32_t shift,
+                            const uint32_t* digit_offset, uint32_t* lookback, uint32_t* ticket,
+                            uint32_t* err);
+cudaError_t launch_ranges(cudaStream_t s, const uint32_t* sorted_key, uint32_t n, uint2* ranges);
+cudaError_t launch_query(cudaStream_t s, uint32_t cap, const uint32_t* sorted_slot, const float2* pos,
+                         const uint32_t* slot_id, const uint2* ranges, TileGrid grid, uint32_t n,
+                         uint32_t* count, uint32_t* list, unsigned long long* pairs);
+cudaError_t launch_iota(cudaStream_t s, uint32_t* out, uint32_t n);
+cudaError_t launch_permute(cudaStream_t s, const uint32_t* sorted_slot, EntityState src,
+                           EntityState dst, uint32_t n);
+cudaError_t launch_export_state(cudaStream_t s, EntityState st, uint32_t n, float2* pos,
+                                uint32_t* head, uint4* rng, float* speed);
+cudaError_t launch_export_neighbours(cudaStream_t s, const uint32_t* sorted_slot, const uint32_t* slot_id,
+                                     const uint32_t* count, const uint32_t* list, uint32_t n,
+                                     uint32_t cap, uint32_t* out_count, uint32_t* out_idx);
+cudaError_t launch_export_aos(cudaStream_t s, const DeviceMap& m, EntityState st, uint32_t n, float dt,
+                              const uint32_t* sorted_slot, const uint32_t* count, void* out);
+
+int query_smem_bytes(uint32_t cap);
+cudaError_t configure_kernels(uint32_t cap);
+int step_blocks_for(int device, uint32_t n);
+
+}  // namespace msim

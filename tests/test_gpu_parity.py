@@ -1,0 +1,264 @@
+"""Per-tick parity of the CUDA path (through the C ABI) against the CPU oracle.
+
+Integer state (headings, RNG states, neighbour ids and counts) must be equal;
+positions are compared bit for bit (the move step has no FMA contraction and
+uses correctly rounded divide and square root, so the tolerance is 0 m).
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+POS_TOL_M = 0.0  # bit-exact
+
+
+def _assert_state(st, pos, head, rng, what=""):
+    assert np.array_equal(st["heading"], head), f"headings differ {what}"
+    assert np.array_equal(st["rng"], rng), f"RNG states differ {what}"
+    if POS_TOL_M == 0.0:
+        bad = np.nonzero(st["pos"].view(np.uint32) != pos.view(np.uint32))[0]
+        assert bad.size == 0, f"positions differ {what}: first at entity {bad[:5]} {st['pos'][bad[:3]]} vs {pos[bad[:3]]}"
+    else:
+        np.testing.assert_allclose(st["pos"], pos, atol=POS_TOL_M, rtol=0)
+
+
+def _oracle_state(orc, road_map, n, rng_kind, seed, placement, speed):
+    return orc.init_entities(road_map.road_pos, n, rng_kind, seed, placement, speed[0], speed[1])
+
+
+@pytest.mark.parametrize("rng_name,rng_kind", [("xorshift128", 0), ("pcg32", 1)])
+@pytest.mark.parametrize("placement,pl", [("start", 0), ("fraction", 1)])
+def test_init_matches_oracle(msim, orc, rng_name, rng_kind, placement, pl):
+    road_map = msim.RoadMap.lattice(24, 3)
+    n = 5000
+    with msim.Simulation(road_map, n, rng=rng_name, dt=0.1, radius=2.0) as sim:
+        sim.init_entities(99, placement=placement, speed=(1.0, 1.6))
+        st = sim.get_state()
+    pos, head, rng, speed = _oracle_state(orc, road_map, n, rng_kind, 99, pl, (1.0, 1.6))
+    _assert_state(st, pos, head, rng, "after init")
+    assert np.array_equal(st["speed"].view(np.uint32), speed.view(np.uint32))
+
+
+@pytest.mark.parametrize("rng_name,rng_kind", [("xorshift128", 0), ("pcg32", 1)])
+def test_plain_config_1000_ticks(msim, orc, rng_name, rng_kind):
+    """Plain config: 10,000 entities on the 32x32 lattice, 1,000 ticks at dt = 0.1."""
+    road_map = msim.RoadMap.lattice(32, 20261203)
+    n, ticks = 10_000, 1000
+    with msim.Simulation(road_map, n, rng=rng_name, dt=0.1, radius=2.0, cap=64) as sim:
+        sim.init_entities(20261203, placement="fraction", speed=(1.0, 1.6))
+        pos, head, rng, speed = _oracle_state(orc, road_map, n, rng_kind, 20261203, 1, (1.0, 1.6))
+        # first per tick, then in multi-tick launches
+        for t in range(20):
+            sim.step(1)
+            orc.step(road_map.road_pos, road_map.road_conn, road_map.connections, pos, head, rng, speed, rng_kind, 0.1, 1)
+            _assert_state(sim.get_state(), pos, head, rng, f"at tick {t + 1}")
+        sim.step(ticks - 20)
+        orc.step(road_map.road_pos, road_map.road_conn, road_map.connections, pos, head, rng, speed, rng_kind, 0.1,
+                 ticks - 20, threads=8)
+        _assert_state(sim.get_state(), pos, head, rng, f"at tick {ticks}")
+        assert sim.tick == ticks
+    # the run must have exercised road-end events with random choices
+    assert np.any(rng != _oracle_state(orc, road_map, n, rng_kind, 20261203, 1, (1.0, 1.6))[2])
+
+
+@pytest.mark.parametrize("rng_name,rng_kind,resort", [("pcg32", 1, 3), ("xorshift128", 0, 1), ("pcg32", 1, 1000)])
+def test_neighbour_ticks_every_tick(msim, orc, rng_name, rng_kind, resort):
+    """Move + index + neighbour query, compared every tick (states, counts, id lists)."""
+    road_map = msim.RoadMap.lattice(20, 5)
+    n, ticks, cap, radius = 12_345, 40, 64, 2.0
+    with msim.Simulation(road_map, n, rng=rng_name, dt=0.1, radius=radius, cap=cap, resort_interval=resort) as sim:
+        sim.init_entities(7, placement="fraction", speed=(1.0, 1.6))
+        pos, head, rng, speed = _oracle_state(orc, road_map, n, rng_kind, 7, 1, (1.0, 1.6))
+        for t in range(ticks):
+            sim.step(1, neighbours=True)
+            orc.step(road_map.road_pos, road_map.road_conn, road_map.connections, pos, head, rng, speed, rng_kind, 0.1, 1)
+            _assert_state(sim.get_state(), pos, head, rng, f"at tick {t + 1}")
+            cnt, idx = sim.get_neighbours()
+            ocnt, oidx, opairs = orc.neighbours(pos, radius, cap, threads=8)
+            assert np.array_equal(cnt, ocnt), f"neighbour counts differ at tick {t + 1}"
+            assert np.array_equal(idx, oidx), f"neighbour lists differ at tick {t + 1}"
+            assert sim.collision_pairs() == opairs
+        assert cnt.sum() > 0
+
+
+def test_reference_mode_test_map(msim, orc):
+    """test_map.json semantics: SPEED 1.4 per tick, xorshift128, R = 10, including the
+    draw that reads one past the connection list (pad entry)."""
+    import json
+    from pathlib import Path
+
+    g = np.load(Path(__file__).parent / "golden" / "test_map.npz")
+    road_map = msim.RoadMap(g["road_pos"], g["road_conn"], g["connections"], float(g["width"]), float(g["height"]))
+    n, ticks = 2000, 300
+    with msim.Simulation(road_map, n, rng="xorshift128", dt=1.0, radius=10.0, cap=16, resort_interval=4) as sim:
+        sim.init_entities(1, placement="start", speed=(1.4, 1.4))
+        pos, head, rng, speed = _oracle_state(orc, road_map, n, 0, 1, 0, (1.4, 1.4))
+        for t in range(ticks):
+            sim.step(1, neighbours=True)
+            orc.step(road_map.road_pos, road_map.road_conn, road_map.connections, pos, head, rng, speed, 0, 1.0, 1)
+            if t % 10 == 9:
+                _assert_state(sim.get_state(), pos, head, rng, f"at tick {t + 1}")
+                cnt, idx = sim.get_neighbours()
+                ocnt, oidx, _ = orc.neighbours(pos, 10.0, 16, threads=8)
+                assert np.array_equal(cnt, ocnt) and np.array_equal(idx, oidx)
+        # every road must have been used
+        assert set(np.unique(head & 0x7FFFFFFF)) == {0, 1, 2, 3}
+
+
+def test_plain_neighbours_config_sampled(msim, orc):
+    """1,000,000 entities on the 256x256 lattice, R = 2.0, cap 64: state and
+    neighbour sets after 10 ticks (the full 500-tick run is in bench.py)."""
+    road_map = msim.RoadMap.lattice(256, 20261203)
+    n, ticks = 1_000_000, 10
+    with msim.Simulation(road_map, n, rng="pcg32", dt=0.1, radius=2.0, cap=64) as sim:
+        sim.init_entities(20261203, placement="fraction", speed=(1.0, 1.6))
+        pos, head, rng, speed = _oracle_state(orc, road_map, n, 1, 20261203, 1, (1.0, 1.6))
+        sim.step(ticks, neighbours=True)
+        orc.step(road_map.road_pos, road_map.road_conn, road_map.connections, pos, head, rng, speed, 1, 0.1, ticks,
+                 threads=16)
+        _assert_state(sim.get_state(), pos, head, rng, f"at tick {ticks}")
+        cnt, idx = sim.get_neighbours()
+        ocnt, oidx, opairs = orc.neighbours(pos, 2.0, 64, threads=16)
+        assert np.array_equal(cnt, ocnt)
+        assert np.array_equal(idx, oidx)
+        assert sim.collision_pairs() == opairs
+
+
+def test_edge_cases(msim, orc):
+    road_map = msim.RoadMap.lattice(8, 1)
+    # zero entities
+    with msim.Simulation(road_map, 0, radius=2.0) as sim:
+        sim.init_entities(1)
+        sim.step(3, neighbours=True)
+        sim.step(3)
+        assert sim.get_state()["pos"].shape == (0, 2)
+    # one entity, and a ragged count
+    for n in (1, 4097, 129):
+        with msim.Simulation(road_map, n, rng="pcg32", dt=0.1, radius=2.0, cap=8) as sim:
+            sim.init_entities(3, placement="fraction", speed=(1.0, 1.6))
+            pos, head, rng, speed = _oracle_state(orc, road_map, n, 1, 3, 1, (1.0, 1.6))
+            sim.step(5, neighbours=True)
+            orc.step(road_map.road_pos, road_map.road_conn, road_map.connections, pos, head, rng, speed, 1, 0.1, 5)
+            _assert_state(sim.get_state(), pos, head, rng, f"n={n}")
+            cnt, idx = sim.get_neighbours()
+            ocnt, oidx, _ = orc.neighbours(pos, 2.0, 8)
+            assert np.array_equal(cnt, ocnt) and np.array_equal(idx, oidx)
+
+
+def test_crowd_beyond_cap_and_radius_boundary(msim, orc):
+    """Every entity at one point (count n-1 > cap: the cap smallest ids, ascending) and
+    pairs exactly at distance R (excluded: the predicate is dist < R)."""
+    road_map = msim.RoadMap.lattice(8, 1)
+    n, cap = 300, 64
+    rp = road_map.road_pos
+    # speed 0: positions stay put, so the query sees exactly the set positions
+    pos = np.repeat(rp[:1, :2], n, axis=0).astype(np.float32)
+    pos[200:] = rp[5, :2]
+    pos[250:] = rp[5, :2] + np.float32([2.0, 0.0])  # |dx| == R, dy == 0 -> distance == R -> not in range
+    head = np.full(n, 0x80000000, np.uint32)
+    head[200:] = 5 | 0x80000000
+    rng = np.ones((n, 4), np.uint32)
+    speed = np.zeros(n, np.float32)
+    with msim.Simulation(road_map, n, dt=0.1, radius=2.0, cap=cap) as sim:
+        sim.set_entities(pos, head, rng, speed)
+        sim.step(1, neighbours=True)
+        st = sim.get_state()
+        cnt, idx = sim.get_neighbours()
+    ocnt, oidx, _ = orc.neighbours(st["pos"], 2.0, cap)
+    assert np.array_equal(cnt, ocnt) and np.array_equal(idx, oidx)
+    assert cnt[0] == 199 and np.array_equal(idx[0], np.arange(1, 65))
+    assert cnt[210] == 49  # not the entities at distance exactly R
+
+
+def test_reference_quadtree_golden(msim, golden_dir):
+    """Neighbour lower-counts against the reference's own CPU quad tree
+    (shader_validation), from fixtures generated with the reference code."""
+    g = np.load(golden_dir / "ref_quadtree.npz")
+    for k in range(int(g["cases"])):
+        pos = g[f"pos{k}"]
+        world = g[f"world{k}"]
+        radius = float(g[f"radius{k}"])
+        ref = g[f"lower{k}"]
+        n = pos.shape[0]
+        a, b = np.float32(0.25) * world, np.float32(0.75) * world
+        road_map = msim.RoadMap(np.array([[a[0], a[1], b[0], b[1]]], np.float32), np.zeros((1, 4), np.uint32),
+                                np.zeros(0, np.uint32), float(world[0]), float(world[1]))
+        with msim.Simulation(road_map, n, dt=1.0, radius=radius, cap=256) as sim:
+            sim.set_entities(pos, np.full(n, 0x80000000, np.uint32), np.ones((n, 4), np.uint32),
+                             np.zeros(n, np.float32))
+            sim.step(1, neighbours=True)
+            assert np.array_equal(sim.get_state()["pos"], pos)
+            cnt, idx = sim.get_neighbours()
+        assert cnt.max() <= 256
+        ids = g[f"ids{k}"]
+        for i in range(n):
+            mine = idx[i, : cnt[i]]
+            mine = mine[mine < i]
+            assert mine.size == ref[i], f"case {k} entity {i}: {mine.size} partners below, reference {ref[i]}"
+            assert np.array_equal(mine, ids[i, : ref[i]]), f"case {k} entity {i}: partner ids differ"
+
+
+def test_entities_aos_export(msim, orc):
+    road_map = msim.RoadMap.lattice(12, 2)
+    n = 1000
+    with msim.Simulation(road_map, n, dt=1.0, radius=10.0, cap=8) as sim:
+        sim.init_entities(5)
+        ents = sim.export_entities()
+        assert np.all(ents["color"] == np.float32([1, 0, 0, 1]))
+        sim.step(3, neighbours=True)
+        st = sim.get_state()
+        cnt, _ = sim.get_neighbours()
+        ents = sim.export_entities()
+    assert ents.dtype.itemsize == 64
+    assert np.array_equal(ents["pos"], st["pos"])
+    assert np.array_equal(ents["randomState"], st["rng"])
+    assert np.array_equal(ents["roadIndex"], st["heading"] & 0x7FFFFFFF)
+    assert np.all(ents["initialized"] == 1)
+    rp = road_map.road_pos[ents["roadIndex"]]
+    to_end = (st["heading"] >> 31).astype(bool)
+    target = np.where(to_end[:, None], rp[:, 2:], rp[:, :2])
+    assert np.array_equal(ents["target"], target)
+    blue = np.float32([0, 0, 1, 1])
+    green = np.float32([0, 1, 0, 1])
+    assert np.array_equal(ents["color"][cnt > 0], np.broadcast_to(blue, ((cnt > 0).sum(), 4)))
+    assert np.array_equal(ents["color"][cnt == 0], np.broadcast_to(green, ((cnt == 0).sum(), 4)))
+    d = target - st["pos"]
+    ln = np.sqrt((d * d).sum(1))
+    moving = ln > 0
+    np.testing.assert_allclose(np.sqrt((ents["direction"][moving] ** 2).sum(1)), 1.4, rtol=1e-5)
+
+
+def test_error_paths(msim):
+    road_map = msim.RoadMap.lattice(8, 1)
+    with msim.Simulation(road_map, 10) as sim:
+        with pytest.raises(msim.MsimError) as e:
+            sim.get_neighbours()
+        assert e.value.code == 1
+        bad = np.full(10, road_map.num_roads, np.uint32)
+        with pytest.raises(msim.MsimError) as e:
+            sim.set_entities(np.zeros((10, 2), np.float32), bad, np.ones((10, 4), np.uint32))
+        assert e.value.code == 2
+    broken = msim.RoadMap(road_map.road_pos, road_map.road_conn, road_map.connections.copy(), road_map.width,
+                          road_map.height)
+    broken.connections[0] = 10**6
+    with pytest.raises(msim.MsimError) as e:
+        msim.Simulation(broken, 10)
+    assert e.value.code == 2
+
+
+def test_determinism_and_profiling(msim):
+    road_map = msim.RoadMap.lattice(64, 9)
+    outs = []
+    for _ in range(2):
+        with msim.Simulation(road_map, 50_000, rng="pcg32", dt=0.1, radius=2.0, cap=64, resort_interval=5) as sim:
+            sim.init_entities(4, placement="fraction", speed=(1.0, 1.6))
+            sim.set_profiling(True)
+            sim.step(12, neighbours=True)
+            stats = sim.kernel_stats()
+            outs.append((sim.get_state(), sim.get_neighbours()))
+    assert stats["k_step"]["launches"] == 12 and stats["k_query"]["launches"] == 12
+    assert stats["k_permute"]["launches"] == 2
+    (s0, (c0, i0)), (s1, (c1, i1)) = outs
+    for k in s0:
+        assert np.array_equal(s0[k], s1[k])
+    assert np.array_equal(c0, c1) and np.array_equal(i0, i1)
