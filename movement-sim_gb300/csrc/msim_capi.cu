@@ -295,7 +295,7 @@ int neighbour_tick(msim_ctx* c) {
     CK(cudaMemsetAsync(c->ranges, 0, sizeof(uint2) * c->ranges_count, c->stream), "memset ranges");
     {
         Prof p(c, K_RANGES);
-        CK(launch_ranges(c->stream, c->sorted_key, c->n, c->ranges), "k_ranges");
+        CK(launch_ranges(c->stream, c->sorted_key, c->n, c->ranges, (uint32_t)c->ranges_count), "k_ranges");
     }
     CK(cudaMemsetAsync(c->pairs, 0, sizeof(unsigned long long), c->stream), "memset pairs");
     {

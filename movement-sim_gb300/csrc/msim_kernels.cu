@@ -284,15 +284,21 @@ __global__ __launch_bounds__(kSortThreads) void k_onesweep(const uint32_t* __res
         const uint32_t key = s_keys[i];
         const uint32_t dd = (key >> shift) & 0xffu;
         const uint32_t g = s_global_base[dd] + (i - s_local_start[dd]);
+        if (g >= n) {  // only after a look-back that gave up; never write out of range
+            atomicOr(err, kErrTimeout);
+            continue;
+        }
         keys_out[g] = key;
         vals_out[g] = s_vals[i];
     }
 }
 
-__global__ void k_ranges(const uint32_t* __restrict__ sk, uint32_t n, uint32_t* __restrict__ ranges) {
+__global__ void k_ranges(const uint32_t* __restrict__ sk, uint32_t n, uint32_t* __restrict__ ranges,
+                         uint32_t num_keys) {
     const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= n) return;
     const uint32_t k = sk[p];
+    if (k >= num_keys) return;  // unreachable: keys are Morton codes of clamped tiles
     if (p == 0 || sk[p - 1] != k) ranges[2ull * k] = p;
     if (p + 1 == n || sk[p + 1] != k) ranges[2ull * k + 1] = p + 1;
 }
@@ -315,7 +321,7 @@ __global__ __launch_bounds__(kQueryThreads) void k_query(const uint32_t* __restr
     const uint32_t p = blockIdx.x * kQueryThreads + tid;
     uint32_t count = 0u, lower = 0u;
     if (p < n) {
-        const uint32_t s = sorted_slot[p];
+        const uint32_t s = sorted_slot[p] < n ? sorted_slot[p] : 0u;
         const float2 me = pos[s];
         const uint32_t myid = slot_id[s];
         const uint32_t x0 = tile_coord(__fsub_rn(me.x, g.reach), g.inv_cell, g.tiles_x);
@@ -325,9 +331,10 @@ __global__ __launch_bounds__(kQueryThreads) void k_query(const uint32_t* __restr
         for (uint32_t ty = y0; ty <= y1; ty++) {
             for (uint32_t tx = x0; tx <= x1; tx++) {
                 const uint2 rg = ranges[morton2(tx, ty)];
-                for (uint32_t q = rg.x; q < rg.y; q++) {
+                const uint32_t qend = rg.y < n ? rg.y : n;
+                for (uint32_t q = rg.x; q < qend; q++) {
                     const uint32_t s2 = sorted_slot[q];
-                    if (s2 == s) continue;
+                    if (s2 == s || s2 >= n) continue;
                     if (!in_range(pos[s2], me, g.radius)) continue;
                     const uint32_t oid = slot_id[s2];
                     lower += oid < myid ? 1u : 0u;
@@ -364,7 +371,7 @@ __global__ __launch_bounds__(kQueryThreads) void k_query(const uint32_t* __restr
 __global__ void k_permute(const uint32_t* __restrict__ ss, EntityState src, EntityState dst, uint32_t n) {
     const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= n) return;
-    const uint32_t s = ss[p];
+    const uint32_t s = ss[p] < n ? ss[p] : p;
     dst.pos[p] = src.pos[s];
     dst.head[p] = src.head[s];
     dst.rng[p] = src.rng[s];
@@ -394,6 +401,7 @@ __global__ __launch_bounds__(kQueryThreads) void k_export_nbr(const uint32_t* so
     const uint32_t off = block_exclusive_scan<kQueryThreads>(kept, s_warp, nullptr);
     if (p >= n) return;
     const uint32_t s = sorted_slot ? sorted_slot[p] : p;
+    if (s >= n) return;
     const uint32_t id = slot_id[s];
     if (id >= n) return;
     out_count[id] = c;
@@ -442,6 +450,7 @@ __global__ void k_export_colors(const uint32_t* sorted_slot, const uint32_t* slo
     const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= n) return;
     const uint32_t s = sorted_slot ? sorted_slot[p] : p;
+    if (s >= n) return;
     const uint32_t id = slot_id[s];
     if (id >= n) return;
     const bool hit = count[p] > 0u;
@@ -517,9 +526,9 @@ cudaError_t launch_onesweep(cudaStream_t s, const uint32_t* keys_in, const uint3
     return cudaGetLastError();
 }
 
-cudaError_t launch_ranges(cudaStream_t s, const uint32_t* sorted_key, uint32_t n, uint2* ranges) {
+cudaError_t launch_ranges(cudaStream_t s, const uint32_t* sorted_key, uint32_t n, uint2* ranges, uint32_t num_keys) {
     if (n == 0) return cudaSuccess;
-    k_ranges<<<blocks_for(n, 256), 256, 0, s>>>(sorted_key, n, reinterpret_cast<uint32_t*>(ranges));
+    k_ranges<<<blocks_for(n, 256), 256, 0, s>>>(sorted_key, n, reinterpret_cast<uint32_t*>(ranges), num_keys);
     return cudaGetLastError();
 }
 

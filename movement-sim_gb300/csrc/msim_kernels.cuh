@@ -51,7 +51,7 @@ cudaError_t launch_onesweep(cudaStream_t s, const uint32_t* keys_in, const uint3
                             uint32_t* keys_out, uint32_t* vals_out, uint32_t n, uint32_t shift,
                             const uint32_t* digit_offset, uint32_t* lookback, uint32_t* ticket,
                             uint32_t* err);
-cudaError_t launch_ranges(cudaStream_t s, const uint32_t* sorted_key, uint32_t n, uint2* ranges);
+cudaError_t launch_ranges(cudaStream_t s, const uint32_t* sorted_key, uint32_t n, uint2* ranges, uint32_t num_keys);
 cudaError_t launch_query(cudaStream_t s, uint32_t cap, const uint32_t* sorted_slot, const float2* pos,
                          const uint32_t* slot_id, const uint2* ranges, TileGrid grid, uint32_t n,
                          uint32_t* count, uint32_t* list, unsigned long long* pairs);
