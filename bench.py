@@ -1,0 +1,425 @@
+"""Benchmark of the movement-sim per-tick path on GB300.
+
+A step is one tick over every entity: move (random_move.comp:869-874), spatial
+index rebuild (tile Morton keys, LSD radix sort, tile ranges) and the radius
+neighbour query (random_move.comp:541-719 semantics).  Default workload: the
+scale configuration (16,000,000 entities on a 1024 x 1024 lattice, radius 2 m,
+64 neighbours kept, dt = 0.1 s, PCG32).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--config scale|neighbours|plain]
+
+One JSON line on stdout (rank 0).  Under torchrun every rank runs its own full
+replica (the path is "replicas only" across GPUs: no data-path collective).
+"""
+from __future__ import annotations
+
+import argparse
+import importlib
+import json
+import os
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+SEED = 20261203
+CONFIGS = {
+    # name: lattice side, entities, radius, cap, neighbours, config ticks
+    "plain": dict(lattice=32, entities=10_000, radius=2.0, cap=64, neighbours=False, ticks=1000),
+    "neighbours": dict(lattice=256, entities=1_000_000, radius=2.0, cap=64, neighbours=True, ticks=500),
+    "scale": dict(lattice=1024, entities=16_000_000, radius=2.0, cap=64, neighbours=True, ticks=200),
+}
+DT = 0.1
+SPEED = (1.0, 1.6)
+B_STEP = 24  # algorithmic bytes per entity-step of the move (pos r/w 16, heading 4, speed 4)
+
+
+def b_nbr(k_mean: float) -> float:
+    """Algorithmic bytes per entity of a neighbour tick: (key, id) write 8, sort
+    read 8 + sorted write 8, query read 8, count write 4, 4 per kept neighbour."""
+    return 36.0 + 4.0 * k_mean
+
+
+# per-kernel algorithmic bytes per entity and launch
+KERNEL_BYTES = {
+    "k_step": lambda k: B_STEP + 4,        # move + key write
+    "k_onesweep": lambda k: 16,            # (key, id) read + write
+    "k_ranges": lambda k: 4,               # sorted key read
+    "k_query": lambda k: 12 + 4 * k,       # own pos 8 + count 4 + kept ids
+    "k_permute": lambda k: 72,             # 36-byte state read + write
+    "k_step_multi": lambda k: B_STEP,      # per tick
+    "k_hist_scan": lambda k: 0,
+}
+
+
+def peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def dist_setup(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+
+        backend = "nccl" if torch.cuda.is_available() else "gloo"
+        if backend == "nccl":
+            torch.cuda.set_device(local)
+        dist.init_process_group(backend)
+    return world, rank, local
+
+
+def barrier_sync(world):
+    try:
+        import torch
+
+        if torch.cuda.is_available():
+            torch.cuda.synchronize()
+        if world > 1:
+            import torch.distributed as dist
+
+            dist.barrier()
+    except ImportError:
+        pass
+
+
+def max_over_ranks(value: float, world: int) -> float:
+    if world <= 1:
+        return value
+    import torch
+    import torch.distributed as dist
+
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([value], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = ROOT / "gpurun_out" / f"clocks_{os.getpid()}.csv"
+
+    def __enter__(self):
+        try:
+            self.path.parent.mkdir(exist_ok=True)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.QUERY}",
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=self.f, stderr=subprocess.DEVNULL)
+            time.sleep(0.3)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            self.f.close()
+
+    def summary(self):
+        if not self.proc or not self.path.exists():
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        rows = []
+        for line in self.path.read_text().splitlines():
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                rows.append((float(parts[1]), float(parts[2]), float(parts[3]), parts[4:]))
+            except ValueError:
+                continue
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        for r in rows:
+            for name, v in zip(names, r[3][1:]):
+                if v.lower().startswith("active"):
+                    reasons.add(name)
+        return {"sm_mhz": float(np.median([r[0] for r in rows])), "sm_max_mhz": max(r[1] for r in rows),
+                "power_w_max": max(r[2] for r in rows), "samples": len(rows), "reasons": sorted(reasons)}
+
+
+def make_sim(pkg, cfg, road_map):
+    sim = pkg.Simulation(road_map, cfg["entities"], rng="pcg32", dt=DT, radius=cfg["radius"], cap=cfg["cap"])
+    sim.init_entities(SEED, placement="fraction", speed=SPEED)
+    return sim
+
+
+def run_ours(args, cfg, world, rank, local):
+    pkg = importlib.import_module("movement-sim_gb300")
+    road_map = pkg.RoadMap.lattice(cfg["lattice"], SEED)
+    n = cfg["entities"]
+    nbr = cfg["neighbours"]
+    sim = make_sim(pkg, cfg, road_map)
+    info = sim.info()
+    tick = lambda k: sim.step(k, neighbours=nbr)  # noqa: E731
+
+    # warm-up
+    tick(args.warmup)
+    sim.sync()
+    # timed region: K steps, barrier + sync on both sides, CUDA events on the context stream
+    launches0 = sim.launch_count()
+    with ClockSampler(local) as clocks:
+        barrier_sync(world)
+        sim.timer_begin()
+        if nbr:
+            tick(args.steps)
+        else:  # the move-only path runs many ticks per launch
+            tick(args.steps)
+        ms = sim.timer_end()
+        sim.sync()
+        barrier_sync(world)
+    launches = sim.launch_count() - launches0
+    ms_max = max_over_ranks(ms, world)
+    value = world * n * args.steps / (ms_max / 1e3)
+
+    # mean kept neighbours of the last tick
+    k_mean = 0.0
+    if nbr:
+        cnt, _ = sim.get_neighbours(with_idx=False)
+        k_mean = float(np.minimum(cnt, cfg["cap"]).mean())
+
+    # per-kernel times (separate profiled pass: events around every launch)
+    sim.set_profiling(True)
+    sim.reset_kernel_stats()
+    prof_steps = max(1, min(args.steps, 50))
+    tick(prof_steps)
+    stats = sim.kernel_stats()
+    sim.set_profiling(False)
+    total_ms = sum(v["ms"] for v in stats.values()) or 1.0
+    peak, peak_kind = peaks()
+    kernels = {}
+    for name, v in stats.items():
+        avg = v["ms"] / v["launches"]
+        if name == "k_step_multi":  # several ticks per launch
+            per_launch_bytes = B_STEP * n * prof_steps / v["launches"]
+        else:
+            per_launch_bytes = KERNEL_BYTES.get(name, lambda k: 0)(k_mean) * n
+        kernels[name] = {"launches": v["launches"], "avg_ms": avg, "share": v["ms"] / total_ms,
+                         "algo_bytes_per_launch": per_launch_bytes,
+                         "achieved_gbs": per_launch_bytes / (avg / 1e3) / 1e9 if avg > 0 else None}
+    dominant = max(kernels.items(), key=lambda kv: kv[1]["share"])
+    traffic = None
+    tfile = ROOT / "profiles" / "ncu_traffic.json"
+    if tfile.exists():
+        t = json.loads(tfile.read_text()).get(args.config, {}).get(dominant[0])
+        if t is not None:
+            traffic = t["bytes_per_entity"] * n
+    ach = dominant[1]["achieved_gbs"] or 0.0
+    roofline = {"bound": "hbm", "kernel": dominant[0], "achieved": round(ach, 1), "peak": peak, "unit": "GB/s",
+                "frac": round(ach / peak, 4), "traffic": traffic, "peak_source": peak_kind}
+    tick_bytes = (B_STEP + (b_nbr(k_mean) if nbr else 0.0)) * n
+    tick_gbs = tick_bytes * args.steps / (ms / 1e3) / 1e9
+    roofline_tick = {"achieved": round(tick_gbs, 1), "peak": peak, "unit": "GB/s", "frac": round(tick_gbs / peak, 4),
+                     "algo_bytes_per_entity_step": B_STEP + (b_nbr(k_mean) if nbr else 0.0)}
+
+    # end to end through the C ABI with host buffers: upload the entity state from
+    # pinned memory, run one tick, read the state and neighbour counts back
+    e2e = None
+    if not args.no_e2e:
+        e2e = run_e2e(pkg, sim, cfg, n, nbr, world, min(args.steps, args.e2e_steps))
+    sim.close()
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        cpu = cpu_baseline(cfg, road_map, budget_s=args.cpu_budget)
+    return {
+        "value": value, "ms_per_step": ms_max / args.steps, "clocks": clocks.summary(), "k_mean": k_mean,
+        "roofline": roofline, "roofline_tick": roofline_tick, "kernels": kernels, "e2e": e2e, "cpu": cpu,
+        "launches": launches, "info": info, "roads": road_map.num_roads,
+    }
+
+
+def run_e2e(pkg, sim, cfg, n, nbr, world, steps):
+    pos = pkg.PinnedBuffer((n, 2), np.float32)
+    head = pkg.PinnedBuffer(n, np.uint32)
+    rng = pkg.PinnedBuffer((n, 4), np.uint32)
+    speed = pkg.PinnedBuffer(n, np.float32)
+    cnt = pkg.PinnedBuffer(n, np.uint32)
+    out = {"pos": pos.array, "heading": head.array, "rng": rng.array, "speed": speed.array}
+    sim.get_state(out)
+    L = pkg.lib()
+    ctx = sim._ctx
+    u32 = lambda b: b.array.ctypes.data_as(pkg._capi.u32p)  # noqa: E731
+    f32 = lambda b: b.array.ctypes.data_as(pkg._capi.f32p)  # noqa: E731
+    flags = pkg._capi.STEP_NEIGHBOURS if nbr else 0
+
+    def one():
+        pkg.check(L.msim_set_entities(ctx, f32(pos), u32(head), u32(rng), f32(speed)))
+        pkg.check(L.msim_step(ctx, 1, flags))
+        pkg.check(L.msim_get_state(ctx, f32(pos), u32(head), u32(rng), None))
+        if nbr:
+            pkg.check(L.msim_get_neighbours(ctx, u32(cnt), None))
+
+    one()
+    barrier_sync(world)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        one()
+    barrier_sync(world)
+    dt = max_over_ranks(time.perf_counter() - t0, world)
+    h2d = n * (8 + 4 + 16 + 4)
+    d2h = n * (8 + 4 + 16 + (4 if nbr else 0))
+    for b in (pos, head, rng, speed, cnt):
+        b.free()
+    return {"value": world * n * steps / dt, "unit": "entity-steps/s", "h2d_bytes_per_step": h2d,
+            "d2h_bytes_per_step": d2h, "steps": steps,
+            "path": "msim_set_entities (pinned host) + msim_step(1) + msim_get_state + msim_get_neighbours(counts)"}
+
+
+def oracle_tick_loop(orc, road_map, state, cfg, ticks, threads):
+    pos, head, rng, speed = state
+    for _ in range(ticks):
+        orc.step(road_map.road_pos, road_map.road_conn, road_map.connections, pos, head, rng, speed, 1, DT, 1,
+                 threads=threads)
+        if cfg["neighbours"]:
+            orc.neighbours(pos, cfg["radius"], cfg["cap"], threads=threads, with_idx=True)
+
+
+def cpu_sample_config(cfg):
+    """A bounded sample of the workload for the host cores: at most 2M entities at the
+    workload's density (entities per road), on a correspondingly smaller lattice."""
+    if cfg["entities"] <= 2_000_000:
+        return dict(cfg), "full workload"
+    scale = cfg["entities"] // 2_000_000
+    side = int(round(cfg["lattice"] / np.sqrt(scale)))
+    s = dict(cfg, lattice=side, entities=cfg["entities"] // scale)
+    return s, f"{s['entities']} entities on a {side}x{side} lattice (same entities per road as the workload)"
+
+
+def cpu_baseline(cfg, road_map, budget_s=20.0, kind="port"):
+    from oracle import oracle as orc
+
+    threads = orc.cpu_count()
+    sample, desc = cpu_sample_config(cfg)
+    pkg = importlib.import_module("movement-sim_gb300")
+    rm = road_map if sample["lattice"] == cfg["lattice"] else pkg.RoadMap.lattice(sample["lattice"], SEED)
+    n = sample["entities"]
+    state = orc.init_entities(rm.road_pos, n, 1, SEED, 1, SPEED[0], SPEED[1])
+    oracle_tick_loop(orc, rm, state, sample, 1, threads)  # warm-up tick
+    ticks = 0
+    t0 = time.perf_counter()
+    while True:
+        oracle_tick_loop(orc, rm, state, sample, 1, threads)
+        ticks += 1
+        el = time.perf_counter() - t0
+        if el > budget_s or ticks >= (sample["ticks"]):
+            break
+    return {"value": n * ticks / el, "unit": "entity-steps/s", "cores": threads, "kind": kind,
+            "sample": f"{ticks} ticks of {desc}: oracle C restatement (move + CPU-grid neighbour query), "
+                      f"{threads} threads"}
+
+
+def run_reference(args, cfg, world, rank):
+    """The reference's CPU path restated (the Vulkan shader needs a graphics stack that
+    neither machine has), timed on the host cores: each step is one tick over a
+    bounded sample of the workload."""
+    if rank != 0:
+        return None
+    from oracle import oracle as orc
+
+    pkg = importlib.import_module("movement-sim_gb300")
+    sample, desc = cpu_sample_config(cfg)
+    threads = orc.cpu_count()
+    rm = pkg.RoadMap.lattice(sample["lattice"], SEED)
+    n = sample["entities"]
+    state = orc.init_entities(rm.road_pos, n, 1, SEED, 1, SPEED[0], SPEED[1])
+    oracle_tick_loop(orc, rm, state, sample, args.warmup, threads)
+    t0 = time.perf_counter()
+    oracle_tick_loop(orc, rm, state, sample, args.steps, threads)
+    el = time.perf_counter() - t0
+    v = n * args.steps / el
+    return {"value": v, "ms_per_step": el * 1e3 / args.steps, "threads": threads, "sample": desc}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=None)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--config", choices=sorted(CONFIGS), default="scale")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--e2e-steps", type=int, default=10)
+    ap.add_argument("--cpu-budget", type=float, default=15.0)
+    args = ap.parse_args()
+    cfg = CONFIGS[args.config]
+    if args.steps is None:
+        args.steps = cfg["ticks"]
+    args.warmup = max(args.warmup, 3)
+    world, rank, local = dist_setup(args)
+
+    workload = {
+        "scale": "plain+neighbours at scale: 16,000,000 entities, 1024x1024 lattice, radius 2.0 m, cap 64",
+        "neighbours": "plain+neighbours: 1,000,000 entities, 256x256 lattice, radius 2.0 m, cap 64",
+        "plain": "plain: 10,000 entities, 32x32 lattice, move only",
+    }[args.config]
+    config = {"workload": workload, "entities": cfg["entities"], "lattice": cfg["lattice"], "dt_s": DT,
+              "radius_m": cfg["radius"] if cfg["neighbours"] else None, "cap": cfg["cap"] if cfg["neighbours"] else None,
+              "rng": "pcg32", "speed_mps": list(SPEED), "seed": SEED, "ticks_per_step": 1,
+              "parallelism": f"replicas x{world}",
+              "l2": "inputs larger than L2 (entity state 32 B x entities)" if cfg["entities"] * 32 > 129e6
+              else "working set fits in L2 (small config)"}
+    line = {"metric": "entity-steps/s", "unit": "entity-steps/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded lattice road graph and entities)", "config": config}
+
+    if args.impl == "reference":
+        r = run_reference(args, cfg, world, rank)
+        if rank == 0:
+            line.update({"impl": "reference", "value": r["value"], "ms_per_step": r["ms_per_step"],
+                         "cpu_baseline": {"value": r["value"], "unit": "entity-steps/s", "cores": r["threads"],
+                                          "kind": "port",
+                                          "sample": f"each step one tick of {r['sample']}; oracle C restatement "
+                                                    "of random_move.comp (the Vulkan shader itself is unavailable "
+                                                    "on this box: no graphics stack)"},
+                         "e2e": {"value": r["value"], "unit": "entity-steps/s", "h2d_bytes_per_step": 0,
+                                 "d2h_bytes_per_step": 0}})
+            config["parallelism"] = "host cores"
+            print(json.dumps(line), flush=True)
+        return
+
+    r = run_ours(args, cfg, world, rank, local)
+    if rank == 0:
+        config["roads"] = r["roads"]
+        config["tiles"] = [r["info"]["tiles_x"], r["info"]["tiles_y"]]
+        config["cell_m"] = round(r["info"]["cell_size"], 3)
+        config["sort_passes"] = r["info"]["sort_passes"]
+        config["resort_interval"] = r["info"]["resort_interval"]
+        config["mean_kept_neighbours"] = round(r["k_mean"], 4)
+        line.update({"value": r["value"], "ms_per_step": r["ms_per_step"], "roofline": r["roofline"],
+                     "roofline_tick": r["roofline_tick"], "cpu_baseline": r["cpu"], "e2e": r["e2e"],
+                     "clocks": r["clocks"], "gpu_launches": r["launches"],
+                     "kernels": {k: {kk: (round(vv, 5) if isinstance(vv, float) else vv) for kk, vv in v.items()}
+                                 for k, v in r["kernels"].items()}})
+        print(json.dumps(line), flush=True)
+
+
+if __name__ == "__main__":
+    main()

@@ -189,6 +189,9 @@ int msim_export_entities_aos(msim_ctx* ctx, void* out, size_t n);
 /* Number of ticks run since msim_create (one tick = move [+ collision]). */
 int msim_get_tick(msim_ctx* ctx, uint64_t* tick);
 
+/* Kernels this context has launched since msim_create (all kinds). */
+int msim_get_launch_count(msim_ctx* ctx, uint64_t* launches);
+
 /* Device-side timing of the context's kernels (CUDA events on its stream). */
 int msim_set_profiling(msim_ctx* ctx, int enable);
 int msim_reset_kernel_stats(msim_ctx* ctx);

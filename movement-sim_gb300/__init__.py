@@ -210,6 +210,11 @@ class Simulation:
         check(lib().msim_get_info(self._ctx, ctypes.byref(i)))
         return {f: getattr(i, f) for f, _ in _capi.MsimInfo._fields_}
 
+    def launch_count(self) -> int:
+        v = ctypes.c_uint64()
+        check(lib().msim_get_launch_count(self._ctx, ctypes.byref(v)))
+        return v.value
+
     def set_profiling(self, on: bool) -> None:
         check(lib().msim_set_profiling(self._ctx, 1 if on else 0))
 

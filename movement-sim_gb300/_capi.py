@@ -77,6 +77,7 @@ SIGNATURES = {
     "msim_get_collision_pairs": (ctypes.c_int, [vp, ctypes.POINTER(c_u64)]),
     "msim_export_entities_aos": (ctypes.c_int, [vp, vp, ctypes.c_size_t]),
     "msim_get_tick": (ctypes.c_int, [vp, ctypes.POINTER(c_u64)]),
+    "msim_get_launch_count": (ctypes.c_int, [vp, ctypes.POINTER(c_u64)]),
     "msim_set_profiling": (ctypes.c_int, [vp, ctypes.c_int]),
     "msim_reset_kernel_stats": (ctypes.c_int, [vp]),
     "msim_get_kernel_stats": (ctypes.c_int, [vp, c_u32, ctypes.POINTER(c_u64), ctypes.POINTER(ctypes.c_double)]),

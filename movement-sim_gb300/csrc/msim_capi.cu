@@ -87,6 +87,7 @@ struct msim_ctx {
     size_t stage_bytes = 0;
     // profiling
     bool profiling = false;
+    uint64_t launch_count = 0;  // kernels launched since creation
     struct Pending {
         uint32_t kernel;
         cudaEvent_t a, b;
@@ -173,6 +174,7 @@ struct Prof {
     uint32_t k;
     cudaEvent_t a = nullptr;
     Prof(msim_ctx* ctx, uint32_t kernel) : c(ctx), k(kernel) {
+        c->launch_count++;
         if (c->profiling) {
             a = pool_event(c);
             cudaEventRecord(a, c->stream);
@@ -642,6 +644,12 @@ int msim_export_entities_aos(msim_ctx* c, void* out, size_t n) {
 int msim_get_tick(msim_ctx* c, uint64_t* tick) {
     if (!c || !tick) return fail(MSIM_ERR_INVALID, "NULL argument");
     *tick = c->tick;
+    return MSIM_OK;
+}
+
+int msim_get_launch_count(msim_ctx* c, uint64_t* launches) {
+    if (!c || !launches) return fail(MSIM_ERR_INVALID, "NULL argument");
+    *launches = c->launch_count;
     return MSIM_OK;
 }
 

@@ -1,0 +1,183 @@
+"""CPU tests of the host side: the JSON map loader/writer (Map.cpp:28-150,
+generate_map.py:152-160), the lattice generator's connection-list format
+(generate_map.py:234-258), map validation, and the C ABI's exported symbols."""
+import ctypes
+import json
+import re
+import subprocess
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+ROOT = Path(__file__).resolve().parent.parent
+REFERENCE_MAP = Path("/root/reference/test_map.json")
+
+
+def test_header_symbols_exported(msim):
+    decls = re.findall(r"^\s*(?:int|void|uint32_t|const char\*)\s+(msim_\w+)\s*\(",
+                       (ROOT / "include" / "msim.h").read_text(), re.M)
+    assert len(decls) >= 30
+    lib = msim.lib()
+    for name in decls:
+        assert hasattr(lib, name), name
+    out = subprocess.run(["nm", "-D", "--defined-only", str(msim._capi.LIB_PATH)], capture_output=True, text=True)
+    exported = set(re.findall(r" T (msim_\w+)", out.stdout))
+    assert set(decls) <= exported
+    assert msim.lib().msim_version().decode().startswith("msim-gb300")
+
+
+def test_test_map_loader_matches_fixture(msim, golden_dir, tmp_path):
+    g = np.load(golden_dir / "test_map.npz")
+    if REFERENCE_MAP.exists():
+        m = msim.RoadMap.load_json(REFERENCE_MAP)
+    else:  # round trip through the writer when the reference file is absent
+        src = msim.RoadMap(g["road_pos"], g["road_conn"], g["connections"], float(g["width"]), float(g["height"]))
+        src.write_json(tmp_path / "t.json")
+        m = msim.RoadMap.load_json(tmp_path / "t.json")
+    assert np.array_equal(m.road_pos, g["road_pos"])
+    assert np.array_equal(m.road_conn, g["road_conn"])
+    assert np.array_equal(m.connections, g["connections"])
+    assert m.width == float(g["width"]) and m.height == float(g["height"])
+    m.validate()
+
+
+def _write(tmp_path, doc, name="m.json"):
+    p = tmp_path / name
+    p.write_text(json.dumps(doc))
+    return p
+
+
+def _road(s, e, cs=(0, 1), ce=(0, 1)):
+    return {"start": {"lat": 0, "long": 0, "distLat": s[0], "distLong": s[1]},
+            "end": {"lat": 0, "long": 0, "distLat": e[0], "distLong": e[1]},
+            "connIndexStart": cs[0], "connCountStart": cs[1], "connIndexEnd": ce[0], "connCountEnd": ce[1]}
+
+
+def test_loader_semantics(msim, tmp_path):
+    doc = {"maxDistLat": 0.1, "maxDistLong": 200, "roads": [_road((1, 2), (3, 4)), _road((7, 7), (7, 7)),
+                                                             _road((1e-46, 0.3), (5, 6))],
+           "connectionRoadIndexList": [0, 1]}
+    m = msim.RoadMap.load_json(_write(tmp_path, doc))
+    assert m.num_roads == 2  # the zero-length road is skipped (Map.cpp:124-128)
+    assert m.width == float(np.float32(0.1)) and m.height == 200.0
+    assert m.road_pos[1, 0] == np.float32(1e-46) and m.road_pos[1, 1] == np.float32(0.3)
+    assert list(m.connections) == [0, 1]
+
+
+@pytest.mark.parametrize("drop", ["maxDistLat", "maxDistLong", "roads", "connectionRoadIndexList"])
+def test_loader_missing_top_fields(msim, tmp_path, drop):
+    doc = {"maxDistLat": 10, "maxDistLong": 10, "roads": [_road((1, 2), (3, 4))], "connectionRoadIndexList": [0]}
+    del doc[drop]
+    with pytest.raises(msim.MsimError) as e:
+        msim.RoadMap.load_json(_write(tmp_path, doc))
+    assert e.value.code == 1 and drop in str(e.value)
+
+
+@pytest.mark.parametrize("drop", ["connIndexStart", "connCountStart", "start", "connIndexEnd", "connCountEnd", "end"])
+def test_loader_missing_road_fields(msim, tmp_path, drop):
+    r = _road((1, 2), (3, 4))
+    del r[drop]
+    doc = {"maxDistLat": 10, "maxDistLong": 10, "roads": [r], "connectionRoadIndexList": [0]}
+    with pytest.raises(msim.MsimError) as e:
+        msim.RoadMap.load_json(_write(tmp_path, doc))
+    assert e.value.code == 1 and drop in str(e.value)
+
+
+def test_loader_bad_input(msim, tmp_path):
+    with pytest.raises(msim.MsimError) as e:
+        msim.RoadMap.load_json(tmp_path / "does_not_exist.json")
+    assert e.value.code == 6
+    p = tmp_path / "trunc.json"
+    p.write_text('{"maxDistLat": 10, "roads": [')
+    with pytest.raises(msim.MsimError) as e:
+        msim.RoadMap.load_json(p)
+    assert e.value.code == 1
+    doc = {"maxDistLat": 10, "maxDistLong": 10, "roads": [], "connectionRoadIndexList": [-1]}
+    with pytest.raises(msim.MsimError):
+        msim.RoadMap.load_json(_write(tmp_path, doc))
+
+
+def test_validation(msim):
+    m = msim.RoadMap.lattice(6, 2)
+    m.validate()
+    bad = msim.RoadMap(m.road_pos, m.road_conn, m.connections.copy(), m.width, m.height)
+    bad.connections[3] = m.num_roads
+    with pytest.raises(msim.MsimError) as e:
+        bad.validate()
+    assert e.value.code == 2
+    bad = msim.RoadMap(m.road_pos, m.road_conn.copy(), m.connections, m.width, m.height)
+    bad.road_conn[0, 2] = len(m.connections) - 1
+    bad.road_conn[0, 3] = 3
+    with pytest.raises(msim.MsimError) as e:
+        bad.validate()
+    assert e.value.code == 2
+    bad = msim.RoadMap(m.road_pos.copy(), m.road_conn, m.connections, m.width, m.height)
+    bad.road_pos[2, 2:] = bad.road_pos[2, :2]
+    with pytest.raises(msim.MsimError):
+        bad.validate()
+
+
+def _reference_connection_lists(m):
+    """generate_map.py:234-258 restated over the road endpoints: one list per node,
+    incident roads (here ascending), roads ending at the node appended twice."""
+    nodes = {}
+    for r in range(m.num_roads):
+        for end in (0, 1):
+            key = tuple(m.road_pos[r, 2 * end: 2 * end + 2])
+            nodes.setdefault(key, []).append((r, end))
+    return nodes
+
+
+def test_lattice_format(msim):
+    m = msim.RoadMap.lattice(12, 77)
+    nodes = _reference_connection_lists(m)
+    for key, inc in nodes.items():
+        roads = sorted({r for r, _ in inc})
+        # the list position of this node
+        r0, end0 = inc[0]
+        idx = m.road_conn[r0, 2 * end0]
+        expect = []
+        for r in roads:
+            expect.append(r)
+            if tuple(m.road_pos[r, 2:]) == key:
+                expect.append(r)
+        assert list(m.connections[idx: idx + len(expect)]) == expect
+        for r, end in inc:
+            assert m.road_conn[r, 2 * end] == idx
+            assert m.road_conn[r, 2 * end + 1] == len(roads)
+    # lattice geometry: lower node id is the start, coordinates >= 0, inside the world
+    assert np.all(m.road_pos >= 0)
+    assert np.all(m.road_pos[:, 0::2] <= m.width) and np.all(m.road_pos[:, 1::2] <= m.height)
+    lens = np.hypot(m.road_pos[:, 2] - m.road_pos[:, 0], m.road_pos[:, 3] - m.road_pos[:, 1])
+    assert lens.min() > 20 and lens.max() < 80
+    m.validate()
+
+
+def test_lattice_determinism_and_sizes(msim):
+    a = msim.RoadMap.lattice(32, 20261203)
+    b = msim.RoadMap.lattice(32, 20261203)
+    c = msim.RoadMap.lattice(32, 20261204)
+    assert np.array_equal(a.road_pos, b.road_pos) and np.array_equal(a.connections, b.connections)
+    assert not np.array_equal(a.road_pos, c.road_pos)
+    # expected road counts ~ 0.9 * 2L(L-1), largest component kept
+    for side, lo, hi in [(32, 1650, 1790), (128, 28000, 29300)]:
+        assert lo <= msim.RoadMap.lattice(side, 20261203).num_roads <= hi
+
+
+def test_writer_round_trip(msim, tmp_path):
+    m = msim.RoadMap.lattice(20, 5)
+    m.write_json(tmp_path / "l.json")
+    doc = json.loads((tmp_path / "l.json").read_text())
+    assert set(doc) == {"minDistLat", "maxDistLat", "minDistLong", "maxDistLong", "roads", "connectionRoadIndexList"}
+    m2 = msim.RoadMap.load_json(tmp_path / "l.json")
+    assert np.array_equal(m.road_pos, m2.road_pos) and np.array_equal(m.road_conn, m2.road_conn)
+    assert np.array_equal(m.connections, m2.connections) and m.width == m2.width
+
+
+def test_product_does_not_use_the_oracle():
+    """The product package never imports or loads anything under oracle/."""
+    for p in (ROOT / "movement-sim_gb300").rglob("*"):
+        if p.suffix in (".py", ".cu", ".cuh", ".cpp", ".h"):
+            text = p.read_text()
+            assert "oracle" not in re.sub(r"(#|//).*", "", text).lower() or p.name == "build_lib.py", p
