@@ -294,6 +294,10 @@ def run_e2e(pkg, sim, cfg, n, nbr, world, steps):
 
 def oracle_tick_loop(orc, road_map, state, cfg, ticks, threads):
     pos, head, rng, speed = state
+    if not cfg["neighbours"]:  # entities are independent: every thread runs all ticks on its range
+        orc.step(road_map.road_pos, road_map.road_conn, road_map.connections, pos, head, rng, speed, 1, DT, ticks,
+                 threads=threads)
+        return
     for _ in range(ticks):
         orc.step(road_map.road_pos, road_map.road_conn, road_map.connections, pos, head, rng, speed, 1, DT, 1,
                  threads=threads)
@@ -368,8 +372,14 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=10)
     ap.add_argument("--cpu-budget", type=float, default=15.0)
+    ap.add_argument("--entities", type=int, default=None, help="override (profiling runs)")
+    ap.add_argument("--lattice", type=int, default=None, help="override (profiling runs)")
+    ap.add_argument("--cap", type=int, default=None, help="override (profiling runs)")
     args = ap.parse_args()
-    cfg = CONFIGS[args.config]
+    cfg = dict(CONFIGS[args.config])
+    for k in ("entities", "lattice", "cap"):
+        if getattr(args, k) is not None:
+            cfg[k] = getattr(args, k)
     if args.steps is None:
         args.steps = cfg["ticks"]
     args.warmup = max(args.warmup, 3)
@@ -380,6 +390,9 @@ def main():
         "neighbours": "plain+neighbours: 1,000,000 entities, 256x256 lattice, radius 2.0 m, cap 64",
         "plain": "plain: 10,000 entities, 32x32 lattice, move only",
     }[args.config]
+    overrides = {k: getattr(args, k) for k in ("entities", "lattice", "cap") if getattr(args, k) is not None}
+    if overrides:
+        workload += f" [profiling override {overrides}]"
     config = {"workload": workload, "entities": cfg["entities"], "lattice": cfg["lattice"], "dt_s": DT,
               "radius_m": cfg["radius"] if cfg["neighbours"] else None, "cap": cfg["cap"] if cfg["neighbours"] else None,
               "rng": "pcg32", "speed_mps": list(SPEED), "seed": SEED, "ticks_per_step": 1,
