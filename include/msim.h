@@ -186,6 +186,22 @@ int msim_get_collision_pairs(msim_ctx* ctx, uint64_t* pairs);
  * 876); direction is recomputed from pos and target. */
 int msim_export_entities_aos(msim_ctx* ctx, void* out, size_t n);
 
+/* Reference-layout quad tree over the current positions, for
+ * Simulator::get_quad_tree_nodes (Simulator.cpp:149-153).  nodes receives
+ * node_capacity 64-byte records of GpuQuadTree.hpp:14-41, links (may be NULL)
+ * num_entities 20-byte records of GpuQuadTree.hpp:44-62.  Entities are inserted in
+ * id order with the rules of random_move.comp:309-371 (QUAD_TREE_MAX_DEPTH 8 and
+ * QUAD_TREE_ENTITY_NODE_CAP 10 in Simulator.hpp:36-37).  node_capacity must hold
+ * the full tree (GpuQuadTree.cpp:12-18: 21845 nodes for depth 8).  Synchronous;
+ * the tree is built on the host. */
+int msim_export_quad_tree(msim_ctx* ctx, uint32_t max_depth, uint32_t node_cap, void* nodes,
+                          uint32_t node_capacity, void* links, uint32_t* nodes_used);
+
+/* The same tree for positions given on the host (2n floats), no context needed. */
+int msim_quad_tree_build(const float* pos, uint32_t n, float width, float height, uint32_t max_depth,
+                         uint32_t node_cap, void* nodes, uint32_t node_capacity, void* links,
+                         uint32_t* nodes_used);
+
 /* Number of ticks run since msim_create (one tick = move [+ collision]). */
 int msim_get_tick(msim_ctx* ctx, uint64_t* tick);
 

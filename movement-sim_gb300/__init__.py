@@ -30,6 +30,36 @@ ENTITY_DTYPE = np.dtype([("color", "<f4", (4,)), ("randomState", "<u4", (4,)), (
                          ("initialized", "<u4")])
 assert ENTITY_DTYPE.itemsize == 64
 
+# GpuQuadTree.hpp:14-41 (64-byte node) and :44-62 (20-byte entity link)
+NODE_DTYPE = np.dtype([("acquireLock", "<i4"), ("writeLock", "<i4"), ("readerLock", "<i4"), ("offsetX", "<f4"),
+                       ("offsetY", "<f4"), ("width", "<f4"), ("height", "<f4"), ("contentType", "<u4"),
+                       ("entityCount", "<u4"), ("first", "<u4"), ("prevNodeIndex", "<u4"), ("nextTL", "<u4"),
+                       ("nextTR", "<u4"), ("nextBL", "<u4"), ("nextBR", "<u4"), ("padding", "<u4")])
+LINK_DTYPE = np.dtype([("nodeIndex", "<u4"), ("typeNext", "<u4"), ("next", "<u4"), ("typePrev", "<u4"),
+                       ("prev", "<u4")])
+assert NODE_DTYPE.itemsize == 64 and LINK_DTYPE.itemsize == 20
+QUAD_TREE_MAX_DEPTH = 8        # Simulator.hpp:36
+QUAD_TREE_ENTITY_NODE_CAP = 10  # Simulator.hpp:37
+
+
+def node_count(max_depth: int) -> int:
+    """GpuQuadTree.cpp:12-18 calc_node_count."""
+    return sum(4 ** i for i in range(max_depth))
+
+
+def build_quad_tree(pos, width: float, height: float, max_depth: int = QUAD_TREE_MAX_DEPTH,
+                    node_cap: int = QUAD_TREE_ENTITY_NODE_CAP):
+    """Reference-layout quad tree of host positions (id-order insertion)."""
+    pos = np.ascontiguousarray(pos, dtype=np.float32).reshape(-1, 2)
+    nodes = np.zeros(node_count(max_depth), NODE_DTYPE)
+    links = np.zeros(pos.shape[0], LINK_DTYPE)
+    used = ctypes.c_uint32()
+    check(lib().msim_quad_tree_build(_ptr(pos, ctypes.c_float), pos.shape[0], width, height, max_depth, node_cap,
+                                     nodes.ctypes.data_as(ctypes.c_void_p), nodes.shape[0],
+                                     links.ctypes.data_as(ctypes.c_void_p), ctypes.byref(used)))
+    return nodes, links, used.value
+
+
 _RNG_KINDS = {"xorshift128": RNG_XORSHIFT128, "pcg32": RNG_PCG32}
 
 
@@ -203,6 +233,15 @@ class Simulation:
         out = np.empty(self.n, ENTITY_DTYPE)
         check(lib().msim_export_entities_aos(self._ctx, out.ctypes.data_as(ctypes.c_void_p), self.n))
         return out
+
+    def export_quad_tree(self, max_depth: int = QUAD_TREE_MAX_DEPTH, node_cap: int = QUAD_TREE_ENTITY_NODE_CAP):
+        """Simulator::get_quad_tree_nodes: (nodes, links, nodes_used) in the reference layout."""
+        nodes = np.zeros(node_count(max_depth), NODE_DTYPE)
+        links = np.zeros(self.n, LINK_DTYPE)
+        used = ctypes.c_uint32()
+        check(lib().msim_export_quad_tree(self._ctx, max_depth, node_cap, nodes.ctypes.data_as(ctypes.c_void_p),
+                                          nodes.shape[0], links.ctypes.data_as(ctypes.c_void_p), ctypes.byref(used)))
+        return nodes, links, used.value
 
     # -- reports / timing ------------------------------------------------------
     def info(self) -> dict:

@@ -76,6 +76,8 @@ SIGNATURES = {
     "msim_get_neighbours": (ctypes.c_int, [vp, u32p, u32p]),
     "msim_get_collision_pairs": (ctypes.c_int, [vp, ctypes.POINTER(c_u64)]),
     "msim_export_entities_aos": (ctypes.c_int, [vp, vp, ctypes.c_size_t]),
+    "msim_export_quad_tree": (ctypes.c_int, [vp, c_u32, c_u32, vp, c_u32, vp, u32p]),
+    "msim_quad_tree_build": (ctypes.c_int, [f32p, c_u32, c_f32, c_f32, c_u32, c_u32, vp, c_u32, vp, u32p]),
     "msim_get_tick": (ctypes.c_int, [vp, ctypes.POINTER(c_u64)]),
     "msim_get_launch_count": (ctypes.c_int, [vp, ctypes.POINTER(c_u64)]),
     "msim_set_profiling": (ctypes.c_int, [vp, ctypes.c_int]),

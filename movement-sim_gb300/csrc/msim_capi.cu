@@ -641,6 +641,17 @@ int msim_export_entities_aos(msim_ctx* c, void* out, size_t n) {
     return sync_and_check(c);
 }
 
+int msim_export_quad_tree(msim_ctx* c, uint32_t max_depth, uint32_t node_cap, void* nodes, uint32_t node_capacity,
+                          void* links, uint32_t* nodes_used) {
+    int rc = check_ctx(c);
+    if (rc != MSIM_OK) return rc;
+    std::vector<float> pos((size_t)c->n * 2);
+    rc = msim_get_state(c, pos.data(), nullptr, nullptr, nullptr);
+    if (rc != MSIM_OK) return rc;
+    return build_quad_tree(pos.data(), c->n, c->world_w, c->world_h, max_depth, node_cap, nodes, node_capacity, links,
+                           nodes_used);
+}
+
 int msim_get_tick(msim_ctx* c, uint64_t* tick) {
     if (!c || !tick) return fail(MSIM_ERR_INVALID, "NULL argument");
     *tick = c->tick;

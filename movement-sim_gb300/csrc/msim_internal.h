@@ -28,6 +28,8 @@ int write_map_json(const msim_map& map, const char* path);
 int generate_lattice(uint32_t side, uint64_t seed, float spacing, float jitter, float keep_prob,
                      MapData& out);
 int validate_map(const msim_map& map);
+int build_quad_tree(const float* pos, uint32_t n, float width, float height, uint32_t max_depth, uint32_t node_cap,
+                    void* nodes_out, uint32_t node_capacity, void* links_out, uint32_t* nodes_used);
 
 // Counter-based draws shared by every deterministic initializer: splitmix64 output
 // function (Steele, Lea, Flood 2014) applied twice, keyed by (seed, stream, i).

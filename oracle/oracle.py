@@ -80,6 +80,8 @@ def ref_lib():
                                      ctypes.c_uint, u32p, u32p, u32p, ctypes.c_uint]
         R.ref_lower_sets.restype = ctypes.c_int
         R.ref_collision_test_1.restype = ctypes.c_int
+        R.ref_export_tree.argtypes = [ctypes.c_uint, f32p, ctypes.c_float, ctypes.c_float, ctypes.c_uint, u32p, u32p]
+        R.ref_export_tree.restype = ctypes.c_int
         _REF = R
     return _REF
 
@@ -165,6 +167,22 @@ def ref_lower_sets(pos, world_w, world_h, radius, node_cap=10, max_ids=256):
     if rc != 0:
         raise ValueError("too many entities for the reference's static arrays")
     return lower, events, ids
+
+
+def ref_export_tree(pos, world_w, world_h, node_cap=10):
+    """The reference quad tree (max depth 8) after inserting pos in order: (nodes
+    (21845, 16) uint32 words, links (n, 5) uint32 words)."""
+    R = ref_lib()
+    if R is None:
+        raise RuntimeError("reference quad tree not built (reference sources absent)")
+    pos = np.ascontiguousarray(pos, dtype=np.float32)
+    nodes = np.zeros((21845, 16), np.uint32)
+    links = np.zeros((pos.shape[0], 5), np.uint32)
+    rc = R.ref_export_tree(pos.shape[0], _p(pos, ctypes.c_float), world_w, world_h, node_cap,
+                           _p(nodes, ctypes.c_uint32), _p(links, ctypes.c_uint32))
+    if rc != 0:
+        raise ValueError("too many entities for the reference's static arrays")
+    return nodes, links
 
 
 def cpu_count() -> int:

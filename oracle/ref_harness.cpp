@@ -7,6 +7,8 @@
 // runs the reference's known-answer test run_collision_detection_test_1
 // (main.cpp:1137-1199).  The reference file is included, not copied; its main()
 // is renamed so this library has no entry point.
+#include <cstring>
+
 #define main msim_reference_shader_validation_main
 #include "main.cpp"  // resolved through -I <reference>/shader_validation/src
 #undef main
@@ -60,6 +62,45 @@ int ref_lower_sets(unsigned n, const float* xy, float world_w, float world_h, fl
             k++;
         }
         lower[i] = k;
+    }
+    return 0;
+}
+
+// The reference's tree after inserting entities 0..n-1 in order (single thread):
+// nodes_out receives NUM_NODES records of 16 words (GpuQuadTree.hpp:14-41 field
+// order), links_out n records of 5 words.
+int ref_export_tree(unsigned n, const float* xy, float world_w, float world_h, unsigned node_cap, unsigned* nodes_out,
+                    unsigned* links_out) {
+    if (build_tree(n, xy, world_w, world_h, 10.0f, node_cap) != 0) return -1;
+    for (size_t k = 0; k < NUM_NODES; k++) {
+        const QuadTreeNodeDescriptor& q = quadTreeNodes[k];
+        unsigned* o = nodes_out + 16 * k;
+        int a = q.acquireLock, w = q.writeLock, r = q.readerLock;
+        std::memcpy(o + 0, &a, 4);
+        std::memcpy(o + 1, &w, 4);
+        std::memcpy(o + 2, &r, 4);
+        std::memcpy(o + 3, &q.offsetX, 4);
+        std::memcpy(o + 4, &q.offsetY, 4);
+        std::memcpy(o + 5, &q.width, 4);
+        std::memcpy(o + 6, &q.height, 4);
+        o[7] = q.contentType;
+        o[8] = q.entityCount;
+        o[9] = q.first;
+        o[10] = q.prevNodeIndex;
+        o[11] = q.nextTL;
+        o[12] = q.nextTR;
+        o[13] = q.nextBL;
+        o[14] = q.nextBR;
+        o[15] = q.padding;
+    }
+    for (unsigned i = 0; i < n; i++) {
+        const QuadTreeEntityDescriptor& e = quadTreeEntities[i];
+        unsigned* o = links_out + 5 * i;
+        o[0] = e.nodeIndex;
+        o[1] = e.typeNext;
+        o[2] = e.next;
+        o[3] = e.typePrev;
+        o[4] = e.prev;
     }
     return 0;
 }

@@ -90,7 +90,21 @@ def ref_quadtree() -> None:
     np.savez(HERE / "ref_quadtree.npz", **out)
 
 
+def ref_tree() -> None:
+    """The reference's quad tree (depth 8, leaf capacity 10) after inserting 1000
+    entities in id order, node and link records as uint32 words."""
+    from oracle import oracle
+
+    rs = np.random.default_rng(7)
+    W, H = np.float32(300.0), np.float32(200.0)
+    pos = rs.uniform([0, 0], [W, H], (1000, 2)).astype(np.float32)
+    pos[500:530] = pos[499]  # a crowd on one point (the same-position rule)
+    nodes, links = oracle.ref_export_tree(pos, float(W), float(H), node_cap=10)
+    np.savez_compressed(HERE / "ref_tree.npz", pos=pos, world=np.float32([W, H]), nodes=nodes, links=links)
+
+
 if __name__ == "__main__":
     test_map()
     ref_quadtree()
+    ref_tree()
     print("fixtures written to", HERE)

@@ -262,3 +262,18 @@ def test_determinism_and_profiling(msim):
     for k in s0:
         assert np.array_equal(s0[k], s1[k])
     assert np.array_equal(c0, c1) and np.array_equal(i0, i1)
+
+
+def test_quad_tree_export_through_context(msim, golden_dir):
+    g = np.load(golden_dir / "ref_tree.npz")
+    pos = g["pos"]
+    n = pos.shape[0]
+    w, h = float(g["world"][0]), float(g["world"][1])
+    road_map = msim.RoadMap(np.float32([[0.25 * w, 0.25 * h, 0.75 * w, 0.75 * h]]), np.zeros((1, 4), np.uint32),
+                            np.zeros(0, np.uint32), w, h)
+    with msim.Simulation(road_map, n, dt=1.0, radius=2.0, cap=8) as sim:
+        sim.set_entities(pos, np.full(n, 0x80000000, np.uint32), np.ones((n, 4), np.uint32), np.zeros(n, np.float32))
+        sim.step(2, neighbours=True)
+        nodes, links, used = sim.export_quad_tree()
+    assert np.array_equal(nodes.view(np.uint32).reshape(-1, 16), g["nodes"])
+    assert np.array_equal(links.view(np.uint32).reshape(-1, 5), g["links"])

@@ -181,3 +181,23 @@ def test_product_does_not_use_the_oracle():
         if p.suffix in (".py", ".cu", ".cuh", ".cpp", ".h"):
             text = p.read_text()
             assert "oracle" not in re.sub(r"(#|//).*", "", text).lower() or p.name == "build_lib.py", p
+
+
+def test_quad_tree_export_matches_reference(msim, orc, golden_dir):
+    """Simulator::get_quad_tree_nodes layout: the sequential id-order tree equals the
+    reference's own CPU tree (shader_validation) node for node and link for link."""
+    g = np.load(golden_dir / "ref_tree.npz")
+    nodes, links, used = msim.build_quad_tree(g["pos"], float(g["world"][0]), float(g["world"][1]), 8, 10)
+    assert np.array_equal(nodes.view(np.uint32).reshape(-1, 16), g["nodes"])
+    assert np.array_equal(links.view(np.uint32).reshape(-1, 5), g["links"])
+    assert used > 1 and nodes["entityCount"].sum() == g["pos"].shape[0]
+    if orc.ref_lib() is not None:
+        rs = np.random.default_rng(9)
+        for cap in (1, 4, 10):
+            pos = rs.uniform(0, [90, 60], (800, 2)).astype(np.float32)
+            pos[300:320] = pos[299]
+            rn, rl = orc.ref_export_tree(pos, 90.0, 60.0, node_cap=cap)
+            mn, ml, _ = msim.build_quad_tree(pos, 90.0, 60.0, 8, cap)
+            assert np.array_equal(mn.view(np.uint32).reshape(-1, 16), rn)
+            assert np.array_equal(ml.view(np.uint32).reshape(-1, 5), rl)
+    assert msim.node_count(8) == 21845 and msim.node_count(1) == 1 and msim.node_count(4) == 85
