@@ -323,7 +323,7 @@ int sync_and_check(msim_ctx* c) {
     uint32_t h = 0;
     CK(cudaMemcpy(&h, c->err, sizeof(h), cudaMemcpyDeviceToHost), "read device status");
     if (h) {
-        CK(cudaMemset(c->err, 0, sizeof(uint32_t)), "clear device status");
+        CK(cudaMemsetAsync(c->err, 0, sizeof(uint32_t), c->stream), "clear device status");
         if (h & kErrTimeout)
             return fail(MSIM_ERR_TIMEOUT, "a bounded device wait (radix sort look-back) gave up; results of the tick are invalid");
         return fail(MSIM_ERR_OOB, "a device-side index check failed (road or connection index out of range)");
@@ -446,15 +446,16 @@ int msim_create(const msim_map* map, const msim_params* params, msim_ctx** out) 
     e = cudaMemcpy(c->road_pos, map->road_pos, sizeof(float4) * c->R, cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemcpy(c->road_conn, map->road_conn, sizeof(uint4) * c->R, cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemcpy(c->conn, conn.data(), sizeof(uint32_t) * (c->C + 1), cudaMemcpyHostToDevice);
-    if (e == cudaSuccess) e = cudaMemset(c->err, 0, sizeof(uint32_t));
+    if (e == cudaSuccess) e = cudaMemsetAsync(c->err, 0, sizeof(uint32_t), c->stream);
     for (int b = 0; b < 2 && e == cudaSuccess; b++) {
-        e = cudaMemset(c->st[b].pos, 0, sizeof(float2) * std::max<size_t>(n, 1));
-        if (e == cudaSuccess) e = cudaMemset(c->st[b].head, 0, sizeof(uint32_t) * std::max<size_t>(n, 1));
-        if (e == cudaSuccess) e = cudaMemset(c->st[b].rng, 0, sizeof(uint4) * std::max<size_t>(n, 1));
-        if (e == cudaSuccess) e = cudaMemset(c->st[b].speed, 0, sizeof(float) * std::max<size_t>(n, 1));
-        if (e == cudaSuccess) e = cudaMemset(c->st[b].slot_id, 0, sizeof(uint32_t) * std::max<size_t>(n, 1));
+        e = cudaMemsetAsync(c->st[b].pos, 0, sizeof(float2) * std::max<size_t>(n, 1), c->stream);
+        if (e == cudaSuccess) e = cudaMemsetAsync(c->st[b].head, 0, sizeof(uint32_t) * std::max<size_t>(n, 1), c->stream);
+        if (e == cudaSuccess) e = cudaMemsetAsync(c->st[b].rng, 0, sizeof(uint4) * std::max<size_t>(n, 1), c->stream);
+        if (e == cudaSuccess) e = cudaMemsetAsync(c->st[b].speed, 0, sizeof(float) * std::max<size_t>(n, 1), c->stream);
+        if (e == cudaSuccess) e = cudaMemsetAsync(c->st[b].slot_id, 0, sizeof(uint32_t) * std::max<size_t>(n, 1), c->stream);
     }
     if (e == cudaSuccess) e = configure_kernels(p.cap);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
     if (e != cudaSuccess) return bail(cuda_fail(e, "context set-up"));
     c->step_blocks = step_blocks_for(c->device, c->n);
     *out = c;

@@ -265,7 +265,9 @@ __global__ __launch_bounds__(kSortThreads) void k_onesweep(const uint32_t* __res
         st_relaxed(my_lb, kFlagPrefix | ((excl + tot) & kValueMask));
     }
     s_global_base[d] = digit_offset[d] + excl;
-    s_local_start[d] = block_exclusive_scan<kSortThreads>(tot, s_warp, nullptr);
+    const uint32_t local_start = block_exclusive_scan<kSortThreads>(tot, s_warp, nullptr);
+    s_local_start[d] = local_start;
+    __syncthreads();  // every thread reads other digits' starts below
 
     // local scatter into shared memory (digit-major), then coalesced runs out
 #pragma unroll
@@ -274,6 +276,10 @@ __global__ __launch_bounds__(kSortThreads) void k_onesweep(const uint32_t* __res
         if (idx < n) {
             const uint32_t dd = (k[r] >> shift) & 0xffu;
             const uint32_t lpos = s_local_start[dd] + s_whist[warp * kRadix + dd] + rk[r];
+            if (lpos >= kSortTile) {  // unreachable: ranks and counts come from the same pass
+                atomicOr(err, kErrOob);
+                continue;
+            }
             s_keys[lpos] = k[r];
             s_vals[lpos] = v[r];
         }

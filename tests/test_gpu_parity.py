@@ -81,6 +81,50 @@ def test_neighbour_ticks_every_tick(msim, orc, rng_name, rng_kind, resort):
         assert cnt.sum() > 0
 
 
+@pytest.mark.parametrize("cell,passes", [(2.05, 3), (6.0, 3), (400.0, 1)])
+def test_sort_pass_counts(msim, orc, cell, passes):
+    """Tile sizes that give 1 and 3 radix passes (20- to 22-bit Morton keys)."""
+    road_map = msim.RoadMap.lattice(64, 13)
+    n, ticks = 150_000, 12
+    with msim.Simulation(road_map, n, rng="pcg32", dt=0.1, radius=2.0, cap=32, cell_size=cell,
+                         resort_interval=5) as sim:
+        assert sim.info()["sort_passes"] == passes
+        sim.init_entities(21, placement="fraction", speed=(1.0, 1.6))
+        pos, head, rng, speed = _oracle_state(orc, road_map, n, 1, 21, 1, (1.0, 1.6))
+        for t in range(ticks):
+            sim.step(1, neighbours=True)
+            orc.step(road_map.road_pos, road_map.road_conn, road_map.connections, pos, head, rng, speed, 1, 0.1, 1,
+                     threads=8)
+            if t % 4 == 3:
+                _assert_state(sim.get_state(), pos, head, rng, f"at tick {t + 1}")
+                cnt, idx = sim.get_neighbours()
+                ocnt, oidx, opairs = orc.neighbours(pos, 2.0, 32, threads=8)
+                assert np.array_equal(cnt, ocnt) and np.array_equal(idx, oidx)
+                assert sim.collision_pairs() == opairs
+
+
+def test_scale_config_full_size(msim, orc):
+    """16,000,000 entities on the 1024x1024 lattice (3 radix passes): states bit-exact
+    and neighbour counts equal to the oracle after 3 neighbour ticks; pair count =
+    half the count sum (symmetry)."""
+    road_map = msim.RoadMap.lattice(1024, 20261203)
+    n, ticks = 16_000_000, 3
+    with msim.Simulation(road_map, n, rng="pcg32", dt=0.1, radius=2.0, cap=64) as sim:
+        assert sim.info()["sort_passes"] == 3
+        sim.init_entities(20261203, placement="fraction", speed=(1.0, 1.6))
+        sim.step(ticks, neighbours=True)
+        st = sim.get_state()
+        cnt, _ = sim.get_neighbours(with_idx=False)
+        pairs = sim.collision_pairs()
+    pos, head, rng, speed = _oracle_state(orc, road_map, n, 1, 20261203, 1, (1.0, 1.6))
+    orc.step(road_map.road_pos, road_map.road_conn, road_map.connections, pos, head, rng, speed, 1, 0.1, ticks,
+             threads=16)
+    _assert_state(st, pos, head, rng, f"at tick {ticks}")
+    ocnt, _, opairs = orc.neighbours(pos, 2.0, 0, threads=16, with_idx=False)
+    assert np.array_equal(cnt, ocnt)
+    assert pairs == opairs and 2 * pairs == int(cnt.sum())
+
+
 def test_reference_mode_test_map(msim, orc):
     """test_map.json semantics: SPEED 1.4 per tick, xorshift128, R = 10, including the
     draw that reads one past the connection list (pad entry)."""
