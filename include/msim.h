@@ -202,6 +202,25 @@ int msim_quad_tree_build(const float* pos, uint32_t n, float width, float height
                          uint32_t node_cap, void* nodes, uint32_t node_capacity, void* links,
                          uint32_t* nodes_used);
 
+/* No counterpart in the reference.  Neighbour sets (same predicate, cap and
+ * ascending order as msim_get_neighbours) for n positions the caller holds on the
+ * device, computed without allocating memory: for callers that cannot call
+ * cudaMalloc at that point (it can synchronise the device and is refused during
+ * stream capture; some hosts own all device memory).  Inputs/outputs are device
+ * pointers: d_pos 2n floats, d_count n words, d_idx n*cap words (may be NULL when
+ * cap is 0), d_status (may be NULL) one word receiving device-side error bits (0 =
+ * ok).  Work is queued on `stream` (a cudaStream_t, NULL = default stream) and not
+ * waited for.  n <= MSIM_NOALLOC_MAX_ENTITIES, else MSIM_ERR_INVALID; tiles are
+ * capped at 512 x 512 over world_w x world_h.  All intermediates live in one
+ * ~7.5 MB static device array per device, held until the process exits; every
+ * call shares it, so calls whose GPU work overlaps race (serialise them).  The
+ * first call on a device looks the array up (cudaGetSymbolAddress) and sets a
+ * kernel attribute: make that first call before any stream capture. */
+#define MSIM_NOALLOC_MAX_ENTITIES 262144u
+int msim_query_neighbours_noalloc(const float* d_pos, uint32_t n, float world_w, float world_h, float radius,
+                                  uint32_t cap, uint32_t* d_count, uint32_t* d_idx, uint32_t* d_status,
+                                  void* stream);
+
 /* Number of ticks run since msim_create (one tick = move [+ collision]). */
 int msim_get_tick(msim_ctx* ctx, uint64_t* tick);
 
