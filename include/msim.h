@@ -243,6 +243,46 @@ int msim_timer_end(msim_ctx* ctx, float* ms);
 int msim_host_alloc(size_t bytes, void** out);
 int msim_host_free(void* ptr);
 
+/* ---- batched ensemble ------------------------------------------------------------
+ * Many independent instances (own road graph and entities each) advanced by one
+ * persistent kernel launch, captured once per tick count into a CUDA graph.  Move
+ * ticks only (no neighbour query); every instance's result is bit-identical to a
+ * single context running msim_step without MSIM_STEP_NEIGHBOURS.  No reference
+ * counterpart: the reference runs one map (Simulator.cpp:44-106). */
+typedef struct msim_batch msim_batch;
+
+#define MSIM_BATCH_MAX_CLASSES 4
+typedef struct msim_batch_schedule {
+    uint32_t block_threads;                                 /* multiple of 32 */
+    uint32_t num_classes;                                   /* size classes, 1..4 */
+    uint32_t class_min_entities[MSIM_BATCH_MAX_CLASSES];    /* class c: min[c] <= n < min[c+1] */
+    uint32_t entities_per_thread[MSIM_BATCH_MAX_CLASSES];   /* 1, 2 or 4 */
+    uint32_t tile_entities[MSIM_BATCH_MAX_CLASSES];         /* entities per work item */
+} msim_batch_schedule;
+
+int msim_batch_default_schedule(msim_batch_schedule* schedule);
+int msim_batch_create(const msim_map* maps, const uint32_t* num_entities, uint32_t count, uint32_t rng_kind,
+                      float dt, msim_batch** out);
+int msim_batch_destroy(msim_batch* batch);
+/* One msim_init per instance (same initializer as msim_init_entities). */
+int msim_batch_init_entities(msim_batch* batch, const msim_init* inits);
+/* Asynchronous: `ticks` move ticks of every instance in one persistent launch. */
+int msim_batch_step(msim_batch* batch, uint32_t ticks);
+int msim_batch_sync(msim_batch* batch);
+int msim_batch_get_state(msim_batch* batch, uint32_t instance, float* pos, uint32_t* heading, uint32_t* rng,
+                         float* speed);
+int msim_batch_set_schedule(msim_batch* batch, const msim_batch_schedule* schedule);
+int msim_batch_get_schedule(msim_batch* batch, msim_batch_schedule* schedule);
+/* Autotuner: times per size class every (entities per thread, tile) candidate, then
+ * the block sizes; keeps the fastest.  The simulation state is left unchanged.
+ * cache_path (may be NULL): a text file of earlier results keyed by device name,
+ * RNG, tick count and instance sizes; a hit skips the timing, a new result is
+ * appended. */
+int msim_batch_tune(msim_batch* batch, uint32_t ticks, const char* cache_path);
+int msim_batch_timer_begin(msim_batch* batch);
+int msim_batch_timer_end(msim_batch* batch, float* ms);
+int msim_batch_info(msim_batch* batch, uint64_t* total_entities, uint32_t* work_items, uint64_t* launches);
+
 /* Resolved configuration of a context (for reports). */
 typedef struct msim_info {
     uint32_t num_entities;

@@ -279,6 +279,101 @@ class Simulation:
         return ms.value
 
 
+def ensemble_config(count: int = 512, seed: int = 20261203, side_range=(16, 256), entity_range=(1_000, 200_000)):
+    """Instance sizes of the batched ensemble: lattice side uniform in side_range
+    (inclusive), entity count log-uniform in entity_range, instance seed = index +
+    seed.  Drawn with numpy's PCG64 generator seeded by `seed`."""
+    rs = np.random.default_rng(seed)
+    sides = rs.integers(side_range[0], side_range[1] + 1, count)
+    lo, hi = np.log(entity_range[0]), np.log(entity_range[1])
+    entities = np.floor(np.exp(rs.uniform(lo, hi, count))).astype(np.int64)
+    seeds = np.arange(count, dtype=np.int64) + seed
+    return [int(x) for x in sides], [int(x) for x in entities], [int(x) for x in seeds]
+
+
+class Batch:
+    """Batched ensemble: independent instances (map, entity count, init) advanced by
+    one persistent launch per msim_batch_step call (move ticks only)."""
+
+    def __init__(self, maps, num_entities, *, rng: str = "pcg32", dt: float = 0.1):
+        self.maps = list(maps)
+        self.n = [int(x) for x in num_entities]
+        views = (_capi.MsimMap * len(self.maps))(*[m.view() for m in self.maps])
+        counts = np.ascontiguousarray(self.n, dtype=np.uint32)
+        self._b = ctypes.c_void_p()
+        check(lib().msim_batch_create(views, _ptr(counts, ctypes.c_uint32), len(self.maps), _RNG_KINDS[rng], dt,
+                                      ctypes.byref(self._b)))
+
+    def close(self):
+        if getattr(self, "_b", None) is not None and self._b.value:
+            lib().msim_batch_destroy(self._b)
+            self._b = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def init_entities(self, seeds, placement: str = "fraction", speed=(1.0, 1.6)):
+        pl = {"start": PLACE_ROAD_START, "fraction": PLACE_UNIFORM_FRACTION}[placement]
+        inits = (_capi.MsimInit * len(self.maps))(*[_capi.MsimInit(seed=int(s), placement=pl, speed_min=speed[0],
+                                                                  speed_max=speed[1]) for s in seeds])
+        check(lib().msim_batch_init_entities(self._b, inits))
+
+    def step(self, ticks: int):
+        check(lib().msim_batch_step(self._b, ticks))
+
+    def sync(self):
+        check(lib().msim_batch_sync(self._b))
+
+    def get_state(self, instance: int):
+        n = self.n[instance]
+        out = {"pos": np.empty((n, 2), np.float32), "heading": np.empty(n, np.uint32),
+               "rng": np.empty((n, 4), np.uint32), "speed": np.empty(n, np.float32)}
+        check(lib().msim_batch_get_state(self._b, instance, _ptr(out["pos"], ctypes.c_float),
+                                         _ptr(out["heading"], ctypes.c_uint32), _ptr(out["rng"], ctypes.c_uint32),
+                                         _ptr(out["speed"], ctypes.c_float)))
+        return out
+
+    def schedule(self) -> dict:
+        s = _capi.MsimBatchSchedule()
+        check(lib().msim_batch_get_schedule(self._b, ctypes.byref(s)))
+        c = s.num_classes
+        return {"block_threads": s.block_threads, "class_min_entities": list(s.class_min_entities[:c]),
+                "entities_per_thread": list(s.entities_per_thread[:c]), "tile_entities": list(s.tile_entities[:c])}
+
+    def set_schedule(self, block_threads, class_min_entities, entities_per_thread, tile_entities):
+        s = _capi.MsimBatchSchedule()
+        s.block_threads = block_threads
+        s.num_classes = len(class_min_entities)
+        for i, (a, b, c) in enumerate(zip(class_min_entities, entities_per_thread, tile_entities)):
+            s.class_min_entities[i], s.entities_per_thread[i], s.tile_entities[i] = a, b, c
+        check(lib().msim_batch_set_schedule(self._b, ctypes.byref(s)))
+
+    def tune(self, ticks: int, cache_path=None):
+        check(lib().msim_batch_tune(self._b, ticks, str(cache_path).encode() if cache_path else None))
+
+    def timer_begin(self):
+        check(lib().msim_batch_timer_begin(self._b))
+
+    def timer_end(self) -> float:
+        ms = ctypes.c_float()
+        check(lib().msim_batch_timer_end(self._b, ctypes.byref(ms)))
+        return ms.value
+
+    def info(self) -> dict:
+        t, w, l = ctypes.c_uint64(), ctypes.c_uint32(), ctypes.c_uint64()
+        check(lib().msim_batch_info(self._b, ctypes.byref(t), ctypes.byref(w), ctypes.byref(l)))
+        return {"total_entities": t.value, "work_items": w.value, "launches": l.value}
+
+
 class PinnedBuffer:
     """Page-locked host memory (cudaMallocHost) viewed as a numpy array."""
 

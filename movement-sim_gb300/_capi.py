@@ -49,6 +49,11 @@ class MsimInit(ctypes.Structure):
     _fields_ = [("seed", c_u64), ("placement", c_u32), ("speed_min", c_f32), ("speed_max", c_f32)]
 
 
+class MsimBatchSchedule(ctypes.Structure):
+    _fields_ = [("block_threads", c_u32), ("num_classes", c_u32), ("class_min_entities", c_u32 * 4),
+                ("entities_per_thread", c_u32 * 4), ("tile_entities", c_u32 * 4)]
+
+
 class MsimInfo(ctypes.Structure):
     _fields_ = [("num_entities", c_u32), ("num_roads", c_u32), ("num_connections", c_u32), ("tiles_x", c_u32),
                 ("tiles_y", c_u32), ("key_bits", c_u32), ("sort_passes", c_u32), ("resort_interval", c_u32),
@@ -90,6 +95,19 @@ SIGNATURES = {
     "msim_host_alloc": (ctypes.c_int, [ctypes.c_size_t, ctypes.POINTER(vp)]),
     "msim_host_free": (ctypes.c_int, [vp]),
     "msim_get_info": (ctypes.c_int, [vp, ctypes.POINTER(MsimInfo)]),
+    "msim_batch_default_schedule": (ctypes.c_int, [ctypes.POINTER(MsimBatchSchedule)]),
+    "msim_batch_create": (ctypes.c_int, [ctypes.POINTER(MsimMap), u32p, c_u32, c_u32, c_f32, ctypes.POINTER(vp)]),
+    "msim_batch_destroy": (ctypes.c_int, [vp]),
+    "msim_batch_init_entities": (ctypes.c_int, [vp, ctypes.POINTER(MsimInit)]),
+    "msim_batch_step": (ctypes.c_int, [vp, c_u32]),
+    "msim_batch_sync": (ctypes.c_int, [vp]),
+    "msim_batch_get_state": (ctypes.c_int, [vp, c_u32, f32p, u32p, u32p, f32p]),
+    "msim_batch_set_schedule": (ctypes.c_int, [vp, ctypes.POINTER(MsimBatchSchedule)]),
+    "msim_batch_get_schedule": (ctypes.c_int, [vp, ctypes.POINTER(MsimBatchSchedule)]),
+    "msim_batch_tune": (ctypes.c_int, [vp, c_u32, ctypes.c_char_p]),
+    "msim_batch_timer_begin": (ctypes.c_int, [vp]),
+    "msim_batch_timer_end": (ctypes.c_int, [vp, f32p]),
+    "msim_batch_info": (ctypes.c_int, [vp, ctypes.POINTER(c_u64), u32p, ctypes.POINTER(c_u64)]),
 }
 
 _LIB = None
