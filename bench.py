@@ -35,10 +35,18 @@ CONFIGS = {
     "batched": dict(lattice=0, entities=0, radius=0.0, cap=0, neighbours=False, ticks=1000),
     "neighbours": dict(lattice=256, entities=1_000_000, radius=2.0, cap=64, neighbours=True, ticks=500),
     "scale": dict(lattice=1024, entities=16_000_000, radius=2.0, cap=64, neighbours=True, ticks=200),
+    "adjoint": dict(lattice=128, entities=262_144, radius=0.0, cap=0, neighbours=False, ticks=2000),
 }
 DT = 0.1
 SPEED = (1.0, 1.6)
 B_STEP = 24  # algorithmic bytes per entity-step of the move (pos r/w 16, heading 4, speed 4)
+ADJ_GRID = (512, 512)
+ADJ_K = 100
+# algorithmic bytes per entity-tick of the calibration step: forward B_step + splat
+# position read 8; backward recompute B_step + splat position read 8 + reverse
+# (position and adjoint read + write) 16
+ADJ_FWD_BYTES = B_STEP + 8
+ADJ_BWD_BYTES = B_STEP + 8 + 16
 
 
 def b_nbr(k_mean: float) -> float:
@@ -51,7 +59,7 @@ def b_nbr(k_mean: float) -> float:
 KERNEL_BYTES = {
     "k_step": lambda k: B_STEP + 4,        # move + key write
     "k_onesweep": lambda k: 16,            # (key, id) read + write
-    "k_ranges": lambda k: 4,               # sorted key read
+    "k_kstart": lambda k: 4,               # sorted key read (+ 4 B per key slot, added below)
     "k_query": lambda k: 12 + 4 * k,       # own pos 8 + count 4 + kept ids
     "k_permute": lambda k: 72,             # 36-byte state read + write
     "k_step_multi": lambda k: B_STEP,      # per tick
@@ -221,6 +229,8 @@ def run_ours(args, cfg, world, rank, local):
             per_launch_bytes = B_STEP * n * prof_steps / v["launches"]
         else:
             per_launch_bytes = KERNEL_BYTES.get(name, lambda k: 0)(k_mean) * n
+            if name == "k_kstart":  # writes one word per key of the key space
+                per_launch_bytes += 4 * (2 ** info["key_bits"] + 1)
         kernels[name] = {"launches": v["launches"], "avg_ms": avg, "share": v["ms"] / total_ms,
                          "algo_bytes_per_launch": per_launch_bytes,
                          "achieved_gbs": per_launch_bytes / (avg / 1e3) / 1e9 if avg > 0 else None}
@@ -356,6 +366,119 @@ def run_batched(args, world, rank, local):
                          "note": "state stays in registers for all ticks of a launch: 28 B per entity per launch"}}
 
 
+def run_adjoint(args, world, rank, local):
+    """Differentiable calibration: one step = forward (2,000 ticks of 262,144 entities
+    with the density splat) + loss + the hand-written adjoint; value = entity-ticks of
+    the step / its time.  Target density from hidden road factors U[0.7, 1.3]."""
+    import torch
+
+    pkg = importlib.import_module("movement-sim_gb300")
+    cal = importlib.import_module("movement-sim_gb300.calibration")
+    cfg = dict(CONFIGS["adjoint"])
+    if args.ticks:
+        cfg["ticks"] = args.ticks
+    rm = pkg.RoadMap.lattice(cfg["lattice"], SEED)
+    n, T = cfg["entities"], cfg["ticks"]
+    G = ADJ_GRID[0] * ADJ_GRID[1]
+    calib = cal.Calibration(rm, n, T, dt=DT, rng="pcg32", checkpoint_interval=ADJ_K, grid=ADJ_GRID, seed=SEED,
+                            placement="fraction", speed=SPEED)
+    rs = np.random.default_rng(SEED)
+    hidden = torch.from_numpy(rs.uniform(0.7, 1.3, rm.num_roads).astype(np.float32)).cuda()
+    target = torch.empty(G, dtype=torch.float32, device="cuda")
+    calib.forward(factor=hidden, density=target)
+    st = calib.initial_state()
+    speed = torch.from_numpy(st["speed"].copy()).cuda()
+    factor = torch.ones(rm.num_roads, dtype=torch.float32, device="cuda")
+    gs = torch.empty(n, dtype=torch.float32, device="cuda")
+    gf = torch.empty(rm.num_roads, dtype=torch.float32, device="cuda")
+
+    def step():
+        loss = calib.forward(speed, factor, target)
+        calib.backward(gs, gf)
+        return loss
+
+    for _ in range(args.warmup):
+        loss0 = step()
+    phases = []
+    with ClockSampler(local) as clocks:
+        barrier_sync(world)
+        calib.timer_begin()
+        for _ in range(args.steps):
+            step()
+            phases.append(calib.phase_times())
+        ms = calib.timer_end()
+        barrier_sync(world)
+    ms_max = max_over_ranks(ms, world)
+    value = world * n * T * args.steps / (ms_max / 1e3)
+    ph = {k: float(np.mean([p[k] for p in phases])) for k in phases[0]}
+    fwd_ms = ph["forward"] + ph["loss"]
+    bwd_ms = ph["backward_sweeps"] + ph["road_reduction"]
+    peak, peak_kind = peaks()
+    S = (T + ADJ_K - 1) // ADJ_K
+    kern = {"k_adj_forward": {"launches": 1, "avg_ms": ph["forward"], "algo_bytes_per_launch": ADJ_FWD_BYTES * n * T},
+            "k_adj_backward": {"launches": S, "avg_ms": ph["backward_sweeps"] / S,
+                               "algo_bytes_per_launch": ADJ_BWD_BYTES * n * ADJ_K}}
+    tot = sum(v["avg_ms"] * v["launches"] for v in kern.values())
+    for v in kern.values():
+        v["share"] = v["avg_ms"] * v["launches"] / tot
+        v["achieved_gbs"] = v["algo_bytes_per_launch"] / (v["avg_ms"] / 1e3) / 1e9
+    dom_name, dom = max(kern.items(), key=lambda kv: kv[1]["share"])
+    roofline = {"bound": "hbm", "kernel": dom_name, "achieved": round(dom["achieved_gbs"], 1), "peak": peak,
+                "unit": "GB/s", "frac": round(dom["achieved_gbs"] / peak, 4), "traffic": None,
+                "peak_source": peak_kind,
+                "note": f"algorithmic bytes per entity-tick: forward {ADJ_FWD_BYTES}, backward {ADJ_BWD_BYTES}"}
+    # end to end through the public API with host buffers: speeds and factors from
+    # pinned host memory, forward + backward, gradients and loss back to the host
+    e2e = None
+    if not args.no_e2e:
+        hs = torch.from_numpy(st["speed"].copy()).pin_memory()
+        hf = torch.ones(rm.num_roads, dtype=torch.float32).pin_memory()
+        ogs = torch.empty(n, dtype=torch.float32).pin_memory()
+        ogf = torch.empty(rm.num_roads, dtype=torch.float32).pin_memory()
+        steps_e = max(1, min(args.steps, 3))
+        barrier_sync(world)
+        t0 = time.perf_counter()
+        for _ in range(steps_e):
+            speed.copy_(hs, non_blocking=True)
+            factor.copy_(hf, non_blocking=True)
+            step()
+            ogs.copy_(gs)
+            ogf.copy_(gf)
+        barrier_sync(world)
+        el = max_over_ranks(time.perf_counter() - t0, world)
+        e2e = {"value": world * n * T * steps_e / el, "unit": "entity-steps/s",
+               "h2d_bytes_per_step": 4 * (n + rm.num_roads), "d2h_bytes_per_step": 4 * (n + rm.num_roads) + 8,
+               "steps": steps_e, "path": "pinned speeds/factors -> Calibration.forward + backward -> pinned gradients"}
+    calib.close()
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        cpu = cpu_adjoint(rm, T, budget_entities=args.cpu_entities)
+    return {"value": value, "ms_per_step": ms_max / args.steps, "clocks": clocks.summary(), "roofline": roofline,
+            "kernels": kern, "phases_ms": ph, "forward_ms": fwd_ms, "backward_ms": bwd_ms,
+            "backward_over_forward": bwd_ms / fwd_ms, "step_over_forward": (fwd_ms + bwd_ms) / fwd_ms,
+            "loss": loss0, "roads": rm.num_roads, "e2e": e2e, "cpu": cpu,
+            "launches": args.steps * (3 + S + 3 + 3 + 2)}
+
+
+def cpu_adjoint(rm, ticks, budget_entities=65536):
+    """The FP64 CPU adjoint (forward, loss, reverse sweep) on a bounded sample of the
+    calibration workload: budget_entities entities over all ticks, host threads."""
+    from oracle import oracle as orc
+
+    threads = orc.cpu_count()
+    n = budget_entities
+    pos, head, rng, speed = orc.init_entities(rm.road_pos, n, 1, SEED, 1, SPEED[0], SPEED[1])
+    state = {"pos": pos, "heading": head, "rng": rng}
+    target = np.zeros(ADJ_GRID[0] * ADJ_GRID[1], np.float32)
+    factor = np.ones(rm.num_roads, np.float32)
+    t0 = time.perf_counter()
+    orc.density_adjoint(rm, state, speed, factor, 1, DT, ticks, ADJ_GRID, target, threads=threads)
+    el = time.perf_counter() - t0
+    return {"value": n * ticks / el, "unit": "entity-steps/s", "cores": threads, "kind": "port",
+            "sample": f"{n} entities x {ticks} ticks of the calibration step (FP64 oracle adjoint: forward, loss "
+                      f"and reverse sweep), {threads} threads"}
+
+
 def oracle_tick_loop(orc, road_map, state, cfg, ticks, threads):
     pos, head, rng, speed = state
     if not cfg["neighbours"]:  # entities are independent: every thread runs all ticks on its range
@@ -412,8 +535,41 @@ def run_reference(args, cfg, world, rank):
     from oracle import oracle as orc
 
     pkg = importlib.import_module("movement-sim_gb300")
-    sample, desc = cpu_sample_config(cfg)
     threads = orc.cpu_count()
+    if args.config == "adjoint":  # each step: the FP64 calibration step on a bounded sample
+        rm = pkg.RoadMap.lattice(cfg["lattice"], SEED)
+        for _ in range(min(args.warmup, 1)):
+            cpu_adjoint(rm, cfg["ticks"], args.cpu_entities)
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            r = cpu_adjoint(rm, cfg["ticks"], args.cpu_entities)
+        el = time.perf_counter() - t0
+        v = args.cpu_entities * cfg["ticks"] * args.steps / el
+        return {"value": v, "ms_per_step": el * 1e3 / args.steps, "threads": threads, "sample": r["sample"],
+                "sample_line": f"each step {r['sample']}"}
+    if args.config == "batched":  # each step: one tick of the first instances (>= 1M entities)
+        sides, ents, seeds = pkg.ensemble_config(args.instances, SEED)
+        chosen, total = [], 0
+        for side, n_i, sd in zip(sides, ents, seeds):
+            if total >= 1_000_000:
+                break
+            rm = pkg.RoadMap.lattice(side, sd)
+            chosen.append((rm, orc.init_entities(rm.road_pos, n_i, 1, sd, 1, SPEED[0], SPEED[1])))
+            total += n_i
+        move = dict(neighbours=False)
+
+        def run(ticks):
+            for rm, state in chosen:
+                oracle_tick_loop(orc, rm, state, move, ticks, threads)
+
+        run(args.warmup)
+        t0 = time.perf_counter()
+        run(args.steps)
+        el = time.perf_counter() - t0
+        desc = f"the first {len(chosen)} ensemble instances ({total} entities), move only"
+        return {"value": total * args.steps / el, "ms_per_step": el * 1e3 / args.steps, "threads": threads,
+                "sample": desc, "sample_line": f"each step one tick of {desc}; oracle C restatement of the move step"}
+    sample, desc = cpu_sample_config(cfg)
     rm = pkg.RoadMap.lattice(sample["lattice"], SEED)
     n = sample["entities"]
     state = orc.init_entities(rm.road_pos, n, 1, SEED, 1, SPEED[0], SPEED[1])
@@ -439,15 +595,17 @@ def main():
     ap.add_argument("--entities", type=int, default=None, help="override (profiling runs)")
     ap.add_argument("--lattice", type=int, default=None, help="override (profiling runs)")
     ap.add_argument("--cap", type=int, default=None, help="override (profiling runs)")
+    ap.add_argument("--ticks", type=int, default=None, help="adjoint config: ticks per step (profiling runs)")
     ap.add_argument("--instances", type=int, default=512, help="batched config: number of instances")
     ap.add_argument("--tune-cache", action="store_true", help="batched config: reuse/append the tuner cache")
+    ap.add_argument("--cpu-entities", type=int, default=65536, help="adjoint config: CPU baseline sample size")
     args = ap.parse_args()
     cfg = dict(CONFIGS[args.config])
-    for k in ("entities", "lattice", "cap"):
+    for k in ("entities", "lattice", "cap", "ticks"):
         if getattr(args, k) is not None:
             cfg[k] = getattr(args, k)
     if args.steps is None:
-        args.steps = cfg["ticks"]
+        args.steps = 5 if args.config == "adjoint" else cfg["ticks"]
     args.warmup = max(args.warmup, 3)
     world, rank, local = dist_setup(args)
 
@@ -456,8 +614,10 @@ def main():
         "neighbours": "plain+neighbours: 1,000,000 entities, 256x256 lattice, radius 2.0 m, cap 64",
         "plain": "plain: 10,000 entities, 32x32 lattice, move only",
         "batched": "batched ensemble: 512 instances, lattice side U{16..256}, entities log-U[1e3, 2e5], move only",
+        "adjoint": "differentiable calibration: 262,144 entities, 128x128 lattice, 2,000 ticks, 512x512 density "
+                   "grid, checkpoints every 100 ticks; one step = forward + loss + adjoint",
     }[args.config]
-    overrides = {k: getattr(args, k) for k in ("entities", "lattice", "cap") if getattr(args, k) is not None}
+    overrides = {k: getattr(args, k) for k in ("entities", "lattice", "cap", "ticks") if getattr(args, k) is not None}
     if overrides:
         workload += f" [profiling override {overrides}]"
     config = {"workload": workload, "entities": cfg["entities"], "lattice": cfg["lattice"], "dt_s": DT,
@@ -476,9 +636,10 @@ def main():
             line.update({"impl": "reference", "value": r["value"], "ms_per_step": r["ms_per_step"],
                          "cpu_baseline": {"value": r["value"], "unit": "entity-steps/s", "cores": r["threads"],
                                           "kind": "port",
-                                          "sample": f"each step one tick of {r['sample']}; oracle C restatement "
-                                                    "of random_move.comp (the Vulkan shader itself is unavailable "
-                                                    "on this box: no graphics stack)"},
+                                          "sample": r.get("sample_line") or
+                                          f"each step one tick of {r['sample']}; oracle C restatement "
+                                          "of random_move.comp (the Vulkan shader itself is unavailable "
+                                          "on this box: no graphics stack)"},
                          "e2e": {"value": r["value"], "unit": "entity-steps/s", "h2d_bytes_per_step": 0,
                                  "d2h_bytes_per_step": 0}})
             config["parallelism"] = "host cores"
@@ -496,6 +657,21 @@ def main():
             line["gpu_launches"] = r["launches"]
             line["cpu_baseline"] = None
             line["e2e"] = None
+            print(json.dumps(line), flush=True)
+        return
+    if args.config == "adjoint":
+        if args.impl == "reference":
+            return
+        r = run_adjoint(args, world, rank, local)
+        if rank == 0:
+            config.update({"roads": r["roads"], "ticks_per_step": cfg["ticks"], "grid": list(ADJ_GRID),
+                           "checkpoint_interval": ADJ_K, "hidden_factors": "U[0.7, 1.3] from the seed",
+                           "l2": "inputs larger than L2 (checkpoints and per-segment history)"})
+            line.update({k: r[k] for k in ("value", "ms_per_step", "clocks", "roofline", "e2e")})
+            line.update({"cpu_baseline": r["cpu"], "gpu_launches": r["launches"], "kernels": r["kernels"],
+                         "phases_ms": r["phases_ms"], "forward_ms": r["forward_ms"], "backward_ms": r["backward_ms"],
+                         "backward_over_forward": r["backward_over_forward"],
+                         "step_over_forward": r["step_over_forward"], "loss": r["loss"]})
             print(json.dumps(line), flush=True)
         return
     r = run_ours(args, cfg, world, rank, local)

@@ -4,7 +4,7 @@
  * The path: every tick each entity moves along its road toward the road end it
  * heads for; at the end it picks the next road from the connection list with its
  * own random state.  After the move, a spatial index over all entities is rebuilt
- * (Morton key of the entity's tile, radix sort, tile ranges) and a radius
+ * (sort key of the entity's tile and y band, radix sort, key-start table) and a radius
  * neighbour query runs over it.
  *
  * Conventions
@@ -282,6 +282,59 @@ int msim_batch_tune(msim_batch* batch, uint32_t ticks, const char* cache_path);
 int msim_batch_timer_begin(msim_batch* batch);
 int msim_batch_timer_end(msim_batch* batch, float* ms);
 int msim_batch_info(msim_batch* batch, uint64_t* total_entities, uint32_t* work_items, uint64_t* launches);
+
+/* ---- differentiable density calibration ------------------------------------------
+ * Forward: `ticks` move ticks of the entities from the deterministic initializer,
+ * step = speed[e] * factor[road] * dt; observable D = (1/ticks) sum_t splat(p_t),
+ * bilinear cell-centred weights on a grid_w x grid_h grid over the world;
+ * loss = mean_g (D_g - target_g)^2.  Backward: the adjoint of the kinematic step
+ * and the splat with the forward's discrete events (road-end ticks and road
+ * choices) held fixed; states are checkpointed every checkpoint_interval ticks and
+ * recomputed; road-factor gradients are summed by a deterministic sort-based
+ * segmented reduction.  Device pointers throughout.  No reference counterpart
+ * (the reference has no differentiable path). */
+typedef struct msim_adj msim_adj;
+typedef struct msim_adj_params {
+    uint32_t num_entities;
+    uint32_t rng_kind;
+    float dt;
+    uint32_t ticks;
+    uint32_t checkpoint_interval; /* K */
+    uint32_t grid_w;
+    uint32_t grid_h;
+    uint32_t placement;           /* MSIM_PLACE_* of the initializer */
+    uint64_t seed;                /* initializer seed */
+    float speed_min;              /* initializer speed range (the speeds a forward without */
+    float speed_max;              /* d_speed uses) */
+} msim_adj_params;
+
+#define MSIM_ADJ_NATURAL 0u /* events from the step itself; the schedule is stored */
+#define MSIM_ADJ_RECORD 1u  /* the same as NATURAL (kept as a name for callers that record) */
+#define MSIM_ADJ_REPLAY 2u  /* force the stored event schedule (finite differences) */
+
+int msim_adj_create(const msim_map* map, const msim_adj_params* params, msim_adj** out);
+int msim_adj_destroy(msim_adj* adj);
+/* Initial state from the initializer (host arrays, any may be NULL). */
+int msim_adj_get_initial_state(msim_adj* adj, float* pos, uint32_t* heading, uint32_t* rng, float* speed);
+/* d_speed (n), d_factor (num_roads), d_target (grid) may be NULL to keep the
+ * previous values (speeds from the initializer, factors 1, target 0); d_density
+ * (grid, may be NULL) receives D; *loss (host, may be NULL).  Synchronous. */
+int msim_adj_forward(msim_adj* adj, const float* d_speed, const float* d_factor, const float* d_target,
+                     float* d_density, uint32_t mode, double* loss);
+/* Gradients of the last forward's loss (device outputs, either may be NULL). */
+int msim_adj_backward(msim_adj* adj, float* d_grad_speed, float* d_grad_factor);
+/* The same gradients as accumulated (double), to host arrays. */
+int msim_adj_get_gradients_f64(msim_adj* adj, double* grad_speed, double* grad_factor);
+/* Event schedule of the last natural forward: one bit per entity and tick (bit
+ * (t-1) % 32 of word (t-1) / 32 set when the entity reaches its road end at tick t),
+ * ceil(ticks/32) words per entity. */
+int msim_adj_get_schedule(msim_adj* adj, uint32_t* words);
+int msim_adj_timer_begin(msim_adj* adj);
+int msim_adj_timer_end(msim_adj* adj, float* ms);
+/* Device time (ms, CUDA events) of the last forward and backward phases:
+ * ms[0] forward kernel, ms[1] loss, ms[2] backward segment sweeps (all segments),
+ * ms[3] road-gradient sort and sums. */
+int msim_adj_phase_times(msim_adj* adj, float ms[4]);
 
 /* Resolved configuration of a context (for reports). */
 typedef struct msim_info {

@@ -28,14 +28,14 @@ enum KernelId : uint32_t {
     K_STEP_MULTI,  // several move-only ticks per launch
     K_HIST_SCAN,
     K_SORT_PASS,
-    K_RANGES,
+    K_KSTART,
     K_QUERY,
     K_PERMUTE,
     K_EXPORT,
     K_COUNT
 };
 static const char* const kKernelNames[K_COUNT] = {"k_init",   "k_step",  "k_step_multi", "k_hist_scan", "k_onesweep",
-                                                  "k_ranges", "k_query", "k_permute",    "k_export"};
+                                                  "k_kstart", "k_query", "k_permute",    "k_export"};
 
 }  // namespace msim
 
@@ -63,8 +63,10 @@ struct msim_ctx {
     uint32_t* digit_off = nullptr;
     uint32_t* lookback = nullptr;
     uint32_t* tickets = nullptr;
-    uint2* ranges = nullptr;
-    size_t ranges_count = 0;
+    uint32_t* kstart = nullptr;  // first sorted position of every key, 2^key_bits + 1 entries
+    uint4* kstart_chunks = nullptr;  // long key gaps, filled by a second kernel
+    uint32_t* kstart_chunk_count = nullptr;
+    size_t num_keys = 0;
     uint32_t sort_tiles = 0;
     const uint32_t* sorted_key = nullptr;
     const uint32_t* sorted_slot = nullptr;
@@ -294,15 +296,18 @@ int neighbour_tick(msim_ctx* c) {
     }
     rc = sort_entities(c, 1);
     if (rc != MSIM_OK) return rc;
-    CK(cudaMemsetAsync(c->ranges, 0, sizeof(uint2) * c->ranges_count, c->stream), "memset ranges");
     {
-        Prof p(c, K_RANGES);
-        CK(launch_ranges(c->stream, c->sorted_key, c->n, c->ranges, (uint32_t)c->ranges_count), "k_ranges");
+        Prof p(c, K_KSTART);
+        uint32_t launched = 0;
+        CK(launch_kstart(c->stream, c->sorted_key, c->n, c->kstart, (uint32_t)c->num_keys, c->kstart_chunks,
+                         c->kstart_chunk_count, &launched),
+           "k_kstart");
+        if (launched > 1) c->launch_count += launched - 1;
     }
-    CK(cudaMemsetAsync(c->pairs, 0, sizeof(unsigned long long), c->stream), "memset pairs");
+    CK(cudaMemsetAsync(c->pairs, 0, sizeof(unsigned long long) * kPairBins, c->stream), "memset pairs");
     {
         Prof p(c, K_QUERY);
-        CK(launch_query(c->stream, c->params.cap, c->sorted_slot, cur_state(c).pos, cur_state(c).slot_id, c->ranges,
+        CK(launch_query(c->stream, c->params.cap, c->kstart, c->sorted_slot, cur_state(c).pos, cur_state(c).slot_id,
                         c->grid, c->n, c->nbr_count, c->nbr_list, c->pairs),
            "k_query");
     }
@@ -411,8 +416,12 @@ int msim_create(const msim_map* map, const msim_params* params, msim_ctx** out) 
     c->grid.bits = bits;
     c->grid.reach = (float)reach;
     c->grid.radius = p.radius;
-    c->passes = (2 * bits + 7) / 8;
-    c->ranges_count = (size_t)1 << (2 * bits);
+    c->grid.d2_limit = sqrt_limit(p.radius);
+    // y bands inside a tile fill the key up to 24 bits (3 radix passes), at most 64 bands
+    c->grid.ybits = std::min<uint32_t>(6u, 24u - 2u * bits);
+    c->grid.ybands = (float)(1u << c->grid.ybits);
+    c->passes = (2 * bits + c->grid.ybits + 7) / 8;
+    c->num_keys = (size_t)1 << (2 * bits + c->grid.ybits);
     c->resort = p.resort_interval ? p.resort_interval : 16u;
     c->sort_tiles = (uint32_t)((c->n + kSortTile - 1) / kSortTile);
     if (c->sort_tiles == 0) c->sort_tiles = 1;
@@ -431,8 +440,9 @@ int msim_create(const msim_map* map, const msim_params* params, msim_ctx** out) 
     if ((rc = dalloc(c, &c->key, n)) || (rc = dalloc(c, &c->hist, (size_t)kMaxPasses * kRadix)) ||
         (rc = dalloc(c, &c->digit_off, (size_t)kMaxPasses * kRadix)) ||
         (rc = dalloc(c, &c->lookback, (size_t)kMaxPasses * c->sort_tiles * kRadix)) ||
-        (rc = dalloc(c, &c->tickets, (size_t)kMaxPasses)) || (rc = dalloc(c, &c->ranges, c->ranges_count)) ||
-        (rc = dalloc(c, &c->nbr_count, n)) || (rc = dalloc(c, &c->pairs, 1)) || (rc = dalloc(c, &c->err, 1)))
+        (rc = dalloc(c, &c->tickets, (size_t)kMaxPasses)) || (rc = dalloc(c, &c->kstart, c->num_keys + 1)) ||
+        (rc = dalloc(c, &c->kstart_chunks, kstart_chunks(c->num_keys))) || (rc = dalloc(c, &c->kstart_chunk_count, 1)) ||
+        (rc = dalloc(c, &c->nbr_count, n)) || (rc = dalloc(c, &c->pairs, kPairBins)) || (rc = dalloc(c, &c->err, 1)))
         return bail(rc);
     if (p.cap > 0) {
         size_t blocks = (n + kQueryThreads - 1) / kQueryThreads;
@@ -618,10 +628,12 @@ int msim_get_collision_pairs(msim_ctx* c, uint64_t* pairs) {
     if (rc != MSIM_OK) return rc;
     if (!pairs) return fail(MSIM_ERR_INVALID, "pairs is NULL");
     if (!c->have_nbr) return fail(MSIM_ERR_INVALID, "no neighbour tick has run since the entities were set");
-    unsigned long long h = 0;
-    CK(cudaMemcpyAsync(&h, c->pairs, sizeof(h), cudaMemcpyDeviceToHost, c->stream), "download pairs");
+    unsigned long long h[kPairBins];
+    CK(cudaMemcpyAsync(h, c->pairs, sizeof(h), cudaMemcpyDeviceToHost, c->stream), "download pairs");
     rc = sync_and_check(c);
-    *pairs = h;
+    uint64_t sum = 0;
+    for (uint32_t b = 0; b < kPairBins; b++) sum += h[b];
+    *pairs = sum;
     return rc;
 }
 
@@ -738,7 +750,7 @@ int msim_get_info(msim_ctx* c, msim_info* out) {
     out->num_connections = c->C;
     out->tiles_x = c->grid.tiles_x;
     out->tiles_y = c->grid.tiles_y;
-    out->key_bits = 2 * c->grid.bits;
+    out->key_bits = 2 * c->grid.bits + c->grid.ybits;
     out->sort_passes = c->passes;
     out->resort_interval = c->resort;
     out->cell_size = 1.f / c->grid.inv_cell;

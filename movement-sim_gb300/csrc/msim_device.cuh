@@ -8,6 +8,7 @@
 // order (src/sim/shader/random_move.comp).
 #pragma once
 
+#include <cmath>
 #include <cstdint>
 #include <cuda_runtime.h>
 
@@ -30,6 +31,9 @@ struct DeviceMap {
 };
 
 // Uniform tile grid over the world [0, W) x [0, H); tile side = 1 / inv_cell.
+// Sort key = (Morton code of the tile << ybits) | y band of the entity inside its
+// tile (2^ybits bands of equal height), so the entities of a tile are sorted by
+// band and a query reads only the bands its box overlaps.
 struct TileGrid {
     float inv_cell;
     uint32_t tiles_x;
@@ -37,6 +41,9 @@ struct TileGrid {
     uint32_t bits;   // Morton bits per axis
     float reach;     // radius + rounding margin used to pick candidate tiles
     float radius;
+    uint32_t ybits;  // y-band bits below the tile code (0 = none)
+    float ybands;    // 2^ybits as a float
+    float d2_limit;  // smallest float t with sqrt_rn(t) >= radius (see in_range_fast)
 };
 
 // ---- RNG -------------------------------------------------------------------
@@ -166,6 +173,14 @@ __host__ __device__ __forceinline__ uint32_t part1by1(uint32_t x) {
 __host__ __device__ __forceinline__ uint32_t morton2(uint32_t x, uint32_t y) {
     return part1by1(x) | (part1by1(y) << 1);
 }
+// Morton code of the tile one step up in x (or y): add 1 to the interleaved x (y)
+// bits, carrying through the other axis' bits.
+__host__ __device__ __forceinline__ uint32_t morton_inc_x(uint32_t m) {
+    return (((m | 0xAAAAAAAAu) + 1u) & 0x55555555u) | (m & 0xAAAAAAAAu);
+}
+__host__ __device__ __forceinline__ uint32_t morton_inc_y(uint32_t m) {
+    return (((m | 0x55555555u) + 2u) & 0xAAAAAAAAu) | (m & 0x55555555u);
+}
 // Tile coordinate: floor(v / cell) clamped to [0, n-1]; NaN maps to 0.  Monotone
 // in v, so a query box [v - reach, v + reach] maps to a tile interval that holds
 // every tile an in-range entity can occupy.
@@ -175,8 +190,19 @@ __device__ __forceinline__ uint32_t tile_coord(float v, float inv, uint32_t n) {
     if (t >= (float)n) return n - 1u;
     return (uint32_t)t;
 }
+// Band of y inside tile row ty: floor((y / cell - ty) * 2^ybits) clamped to the
+// band range.  Monotone in y for a fixed ty, so the bands of an in-range entity
+// lie between the bands of the query box's lower and upper y.
+__device__ __forceinline__ uint32_t y_band(const TileGrid& g, float y, uint32_t ty) {
+    const float f = floorf(__fmul_rn(__fsub_rn(__fmul_rn(y, g.inv_cell), (float)ty), g.ybands));
+    if (!(f >= 0.f)) return 0u;
+    if (f >= g.ybands) return (1u << g.ybits) - 1u;
+    return (uint32_t)f;
+}
 __device__ __forceinline__ uint32_t tile_key(const TileGrid& g, float2 p) {
-    return morton2(tile_coord(p.x, g.inv_cell, g.tiles_x), tile_coord(p.y, g.inv_cell, g.tiles_y));
+    const uint32_t ty = tile_coord(p.y, g.inv_cell, g.tiles_y);
+    const uint32_t t = morton2(tile_coord(p.x, g.inv_cell, g.tiles_x), ty);
+    return g.ybits ? ((t << g.ybits) | y_band(g, p.y, ty)) : t;
 }
 
 // random_move.comp:551-562 quad_tree_in_range(v1 = other, v2 = self, R):
@@ -189,6 +215,26 @@ __device__ __forceinline__ bool in_range(float2 other, float2 self, float r) {
     float ex = __fsub_rn(other.x, self.x);
     float ey = __fsub_rn(other.y, self.y);
     return __fsqrt_rn(__fadd_rn(__fmul_rn(ex, ex), __fmul_rn(ey, ey))) < r;
+}
+
+// The same predicate without the square root and without branches.  The
+// correctly rounded square root is monotone, so sqrt_rn(d2) < r holds exactly
+// when d2 < d2_limit, the smallest float whose rounded root reaches r.
+__device__ __forceinline__ bool in_range_fast(float2 other, float2 self, float r, float d2_limit) {
+    const float ex = __fsub_rn(other.x, self.x);
+    const float ey = __fsub_rn(other.y, self.y);
+    const float d2 = __fadd_rn(__fmul_rn(ex, ex), __fmul_rn(ey, ey));
+    // |fl(a - b)| == |fl(b - a)|: the first two tests are those of in_range
+    return (fabsf(ex) <= r) & (fabsf(ey) <= r) & (d2 < d2_limit);
+}
+
+// Smallest float t >= 0 whose correctly rounded square root is >= r (host side).
+inline float sqrt_limit(float r) {
+    if (!(r > 0.f)) return 0.f;
+    float t = r * r;  // near the boundary; walk to the exact threshold
+    while (t > 0.f && std::sqrt(std::nextafter(t, 0.f)) >= r) t = std::nextafter(t, 0.f);
+    while (std::sqrt(t) < r) t = std::nextafter(t, INFINITY);
+    return t;
 }
 
 }  // namespace msim

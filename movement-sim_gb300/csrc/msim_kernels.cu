@@ -4,11 +4,11 @@
 // order of the last re-ordering):
 //   k_step      move every entity one tick (random_move.comp:869-874), write its
 //               tile Morton key and count the key's radix digits (warp-aggregated
-//               with __match_any_sync, one shared atomic per digit group)
+//               by ballot over runs of equal digits, one shared atomic per run)
 //   k_hist_scan exclusive offsets of each digit pass
 //   k_onesweep  one stable LSD radix pass per 8-bit digit (decoupled look-back,
 //               warp-level multi-split ranking with __match_any_sync)
-//   k_ranges    [start, end) of each occupied tile in the sorted order
+//   k_kstart    key-start table: first sorted position of every key (tile + band)
 //   k_query     radius neighbour query (random_move.comp:541-719 semantics: the
 //               pair predicate of :551-562), count + the cap smallest ids
 // Every few ticks k_permute re-orders the entity state by the sorted order so
@@ -150,12 +150,20 @@ __global__ __launch_bounds__(kStepThreads) void k_step(StepLaunch a) {
             }
         }
         if (KEY) {
+            // Warp-aggregated digit counts.  Slots follow the spatial order of the
+            // last re-ordering, so neighbouring lanes mostly share digits: each run
+            // of equal digits among consecutive lanes adds its length with one
+            // shared atomic, issued by the run's first lane (found by ballot).
             const unsigned vm = __ballot_sync(0xffffffffu, valid);
-            if (valid) {
-                for (uint32_t ps = 0; ps < a.passes; ps++) {
-                    const uint32_t d = (key >> (8u * ps)) & 0xffu;
-                    const unsigned peers = __match_any_sync(vm, d);
-                    if ((int)lane == __ffs(peers) - 1) atomicAdd(&s_hist[ps * kRadix + d], (uint32_t)__popc(peers));
+            for (uint32_t ps = 0; ps < a.passes; ps++) {
+                const uint32_t d = (key >> (8u * ps)) & 0xffu;
+                const uint32_t dprev = __shfl_up_sync(0xffffffffu, d, 1);
+                const bool head = valid && (lane == 0 || d != dprev);
+                const unsigned heads = __ballot_sync(0xffffffffu, head);
+                if (head) {
+                    const unsigned later = heads & ~((2u << lane) - 1u);  // heads after this lane
+                    const uint32_t end = later ? (uint32_t)(__ffs(later) - 1) : (uint32_t)(32 - __clz(vm));
+                    atomicAdd(&s_hist[ps * kRadix + d], end - lane);
                 }
             }
         }
@@ -299,80 +307,82 @@ __global__ __launch_bounds__(kSortThreads) void k_onesweep(const uint32_t* __res
     }
 }
 
+// [start, end) of every occupied tile; the tile of a key is key >> ybits.
 __global__ void k_ranges(const uint32_t* __restrict__ sk, uint32_t n, uint32_t* __restrict__ ranges,
-                         uint32_t num_keys) {
-    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= n) return;
-    const uint32_t k = sk[p];
-    if (k >= num_keys) return;  // unreachable: keys are Morton codes of clamped tiles
-    if (p == 0 || sk[p - 1] != k) ranges[2ull * k] = p;
-    if (p + 1 == n || sk[p + 1] != k) ranges[2ull * k + 1] = p + 1;
+                         uint32_t num_keys, uint32_t ybits) {
+    // four consecutive sorted keys per thread (one 16-byte load when in range)
+    const uint32_t p0 = (blockIdx.x * blockDim.x + threadIdx.x) * 4u;
+    if (p0 >= n) return;
+    uint32_t k[6];  // k[0] = key before p0, k[1..4] = keys p0..p0+3, k[5] = key after
+    k[0] = p0 ? sk[p0 - 1] : 0xffffffffu;
+    if (p0 + 4 <= n) {
+        const uint4 v = *reinterpret_cast<const uint4*>(sk + p0);
+        k[1] = v.x;
+        k[2] = v.y;
+        k[3] = v.z;
+        k[4] = v.w;
+        k[5] = p0 + 4 < n ? sk[p0 + 4] : 0xffffffffu;
+    } else {
+#pragma unroll
+        for (int i = 1; i < 6; i++) k[i] = p0 + i - 1 < n ? sk[p0 + i - 1] : 0xffffffffu;
+    }
+#pragma unroll
+    for (int i = 0; i < 6; i++) k[i] >>= ybits;  // tile codes (the sentinels stay above every tile)
+#pragma unroll
+    for (int i = 1; i <= 4; i++) {
+        const uint32_t p = p0 + i - 1;
+        if (p >= n || k[i] >= num_keys) continue;  // tiles are Morton codes of clamped tile coordinates
+        if (k[i - 1] != k[i]) ranges[2ull * k[i]] = p;
+        if (k[i + 1] != k[i]) ranges[2ull * k[i] + 1] = p + 1;
+    }
 }
 
-// Neighbour query, one thread per sorted position.  Candidates come from every
-// tile overlapping [pos - reach, pos + reach]; the kept list is the cap smallest
-// entity ids in ascending order, built by insertion into a per-thread column of
-// shared memory (column-interleaved: no bank conflicts).  Each block writes its
-// lists contiguously at block * kQueryThreads * cap.
-template <bool LIST>
-__global__ __launch_bounds__(kQueryThreads) void k_query(const uint32_t* __restrict__ sorted_slot,
-                                                         const float2* __restrict__ pos,
-                                                         const uint32_t* __restrict__ slot_id,
-                                                         const uint2* __restrict__ ranges, TileGrid g,
-                                                         uint32_t n, uint32_t cap, uint32_t* __restrict__ count_out,
-                                                         uint32_t* __restrict__ list, unsigned long long* pairs) {
-    extern __shared__ uint32_t s_list[];
-    __shared__ uint32_t s_warp[kQueryThreads / 32 + 1];
-    const uint32_t tid = threadIdx.x;
-    const uint32_t p = blockIdx.x * kQueryThreads + tid;
-    uint32_t count = 0u, lower = 0u;
-    if (p < n) {
-        const uint32_t s = sorted_slot[p] < n ? sorted_slot[p] : 0u;
-        const float2 me = pos[s];
-        const uint32_t myid = slot_id[s];
-        const uint32_t x0 = tile_coord(__fsub_rn(me.x, g.reach), g.inv_cell, g.tiles_x);
-        const uint32_t x1 = tile_coord(__fadd_rn(me.x, g.reach), g.inv_cell, g.tiles_x);
-        const uint32_t y0 = tile_coord(__fsub_rn(me.y, g.reach), g.inv_cell, g.tiles_y);
-        const uint32_t y1 = tile_coord(__fadd_rn(me.y, g.reach), g.inv_cell, g.tiles_y);
-        for (uint32_t ty = y0; ty <= y1; ty++) {
-            for (uint32_t tx = x0; tx <= x1; tx++) {
-                const uint2 rg = ranges[morton2(tx, ty)];
-                const uint32_t qend = rg.y < n ? rg.y : n;
-                for (uint32_t q = rg.x; q < qend; q++) {
-                    const uint32_t s2 = sorted_slot[q];
-                    if (s2 == s || s2 >= n) continue;
-                    if (!in_range(pos[s2], me, g.radius)) continue;
-                    const uint32_t oid = slot_id[s2];
-                    lower += oid < myid ? 1u : 0u;
-                    if (LIST) {
-                        const uint32_t m = count < cap ? count : cap;
-                        if (m < cap || oid < s_list[(cap - 1) * kQueryThreads + tid]) {
-                            uint32_t j = m < cap ? m : cap - 1;
-                            while (j > 0) {
-                                const uint32_t prev = s_list[(j - 1) * kQueryThreads + tid];
-                                if (prev <= oid) break;
-                                s_list[j * kQueryThreads + tid] = prev;
-                                j--;
-                            }
-                            s_list[j * kQueryThreads + tid] = oid;
-                        }
-                    }
-                    count++;
-                }
-            }
+// The ascending list of the kRegKeep smallest ids, kept in registers.
+constexpr int kRegKeep = 4;
+__device__ __forceinline__ void keep_smallest(uint32_t (&r)[kRegKeep], uint32_t id) {
+    if (id >= r[kRegKeep - 1]) return;
+    r[kRegKeep - 1] = id;
+#pragma unroll
+    for (int i = kRegKeep - 1; i > 0; i--) {
+        if (r[i] < r[i - 1]) {
+            const uint32_t t = r[i];
+            r[i] = r[i - 1];
+            r[i - 1] = t;
         }
-        count_out[p] = count;
-    }
-    uint32_t block_lower = 0u;
-    (void)block_exclusive_scan<kQueryThreads>(lower, s_warp, &block_lower);
-    if (tid == 0 && block_lower) atomicAdd(pairs, (unsigned long long)block_lower);
-    if (LIST) {
-        const uint32_t kept = count < cap ? count : cap;
-        const uint32_t off = block_exclusive_scan<kQueryThreads>(kept, s_warp, nullptr);
-        uint32_t* out = list + (size_t)blockIdx.x * kQueryThreads * cap + off;
-        for (uint32_t j = 0; j < kept; j++) out[j] = s_list[j * kQueryThreads + tid];
     }
 }
+
+// Exact ascending list of the cap smallest ids of one entity, written by
+// insertion straight into its output slots; for the rare entities with more
+// than kRegKeep neighbours.
+__device__ __noinline__ void list_overflow(const uint32_t* __restrict__ sorted_slot, const float2* __restrict__ pos,
+                                           const uint32_t* __restrict__ slot_id, const uint32_t* __restrict__ kstart,
+                                           const TileGrid& g, uint32_t n, uint32_t p, float2 me, uint32_t x0,
+                                           uint32_t x1, uint32_t y0, uint32_t y1, uint32_t cap, uint32_t* out) {
+    uint32_t m = 0;
+    for (uint32_t ty = y0; ty <= y1; ty++) {
+        for (uint32_t tx = x0; tx <= x1; tx++) {
+            const uint32_t t = morton2(tx, ty);
+            const uint32_t q0 = kstart[t << g.ybits];
+            const uint32_t q1 = kstart[(t + 1u) << g.ybits];
+            const uint32_t qend = q1 < n ? q1 : n;
+            for (uint32_t q = q0; q < qend; q++) {
+                const uint32_t s2 = sorted_slot[q];
+                if (q == p || s2 >= n || !in_range(pos[s2], me, g.radius)) continue;
+                const uint32_t oid = slot_id[s2];
+                if (m == cap && oid >= out[cap - 1]) continue;
+                uint32_t j = m < cap ? m++ : cap - 1;
+                while (j > 0 && out[j - 1] > oid) {
+                    out[j] = out[j - 1];
+                    j--;
+                }
+                out[j] = oid;
+            }
+        }
+    }
+}
+
+#include "msim_query.cuh"
 
 __global__ void k_permute(const uint32_t* __restrict__ ss, EntityState src, EntityState dst, uint32_t n) {
     const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
@@ -400,11 +410,17 @@ __global__ __launch_bounds__(kQueryThreads) void k_export_nbr(const uint32_t* so
                                                               const uint32_t* count, const uint32_t* list,
                                                               uint32_t n, uint32_t cap, uint32_t* out_count,
                                                               uint32_t* out_idx) {
-    __shared__ uint32_t s_warp[kQueryThreads / 32 + 1];
+    // the query's list layout: warp w's lists at w * 32 * cap, in lane order
     const uint32_t p = blockIdx.x * kQueryThreads + threadIdx.x;
+    const uint32_t lane = threadIdx.x & 31;
     const uint32_t c = p < n ? count[p] : 0u;
     const uint32_t kept = c < cap ? c : cap;
-    const uint32_t off = block_exclusive_scan<kQueryThreads>(kept, s_warp, nullptr);
+    uint32_t incl = kept;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= (uint32_t)o) incl += y;
+    }
     if (p >= n) return;
     const uint32_t s = sorted_slot ? sorted_slot[p] : p;
     if (s >= n) return;
@@ -412,7 +428,7 @@ __global__ __launch_bounds__(kQueryThreads) void k_export_nbr(const uint32_t* so
     if (id >= n) return;
     out_count[id] = c;
     if (out_idx && cap) {
-        const uint32_t* src = list + (size_t)blockIdx.x * kQueryThreads * cap + off;
+        const uint32_t* src = list + (size_t)(p >> 5) * 32u * cap + (incl - kept);
         uint32_t* dst = out_idx + (size_t)id * cap;
         for (uint32_t j = 0; j < cap; j++) dst[j] = j < kept ? src[j] : 0xffffffffu;
     }
@@ -473,16 +489,9 @@ inline unsigned blocks_for(uint32_t n, unsigned threads) { return (unsigned)((n 
 
 }  // namespace
 
-int query_smem_bytes(uint32_t cap) { return (int)(cap * kQueryThreads * sizeof(uint32_t)); }
+int query_smem_bytes(uint32_t) { return 0; }  // the query keeps its lists in registers
 
-cudaError_t configure_kernels(uint32_t cap) {
-    int bytes = query_smem_bytes(cap);
-    if (bytes > 48 * 1024) {
-        cudaError_t e = cudaFuncSetAttribute(k_query<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-        if (e != cudaSuccess) return e;
-    }
-    return cudaSuccess;
-}
+cudaError_t configure_kernels(uint32_t) { return cudaSuccess; }
 
 int step_blocks_for(int device, uint32_t n) {
     int sms = 0, per_sm = 0;
@@ -532,22 +541,54 @@ cudaError_t launch_onesweep(cudaStream_t s, const uint32_t* keys_in, const uint3
     return cudaGetLastError();
 }
 
-cudaError_t launch_ranges(cudaStream_t s, const uint32_t* sorted_key, uint32_t n, uint2* ranges, uint32_t num_keys) {
+cudaError_t launch_ranges(cudaStream_t s, const uint32_t* sorted_key, uint32_t n, uint2* ranges, uint32_t num_keys,
+                          uint32_t ybits) {
     if (n == 0) return cudaSuccess;
-    k_ranges<<<blocks_for(n, 256), 256, 0, s>>>(sorted_key, n, reinterpret_cast<uint32_t*>(ranges), num_keys);
+    k_ranges<<<blocks_for((n + 3) / 4, 256), 256, 0, s>>>(sorted_key, n, reinterpret_cast<uint32_t*>(ranges), num_keys,
+                                                          ybits);
     return cudaGetLastError();
 }
 
-cudaError_t launch_query(cudaStream_t s, uint32_t cap, const uint32_t* sorted_slot, const float2* pos,
-                         const uint32_t* slot_id, const uint2* ranges, TileGrid grid, uint32_t n, uint32_t* count,
-                         uint32_t* list, unsigned long long* pairs) {
+uint32_t kstart_chunks(uint64_t num_keys) { return kstart_chunk_cap(num_keys); }
+
+cudaError_t launch_kstart(cudaStream_t s, const uint32_t* sorted_key, uint32_t n, uint32_t* kstart, uint32_t num_keys,
+                          uint4* chunks, uint32_t* chunk_count, uint32_t* kernels) {
+    if (kernels) *kernels = 0;
+    if (num_keys == 0) return cudaSuccess;
+    if (kernels) *kernels = 1;
+    const uint64_t entries = (uint64_t)num_keys + 1u;
+    if ((uint64_t)n > 8u * entries) {  // many positions per key
+        k_kstart_search<<<(unsigned)((entries + 255u) / 256u), 256, 0, s>>>(sorted_key, n, kstart, num_keys);
+    } else if (chunks && chunk_count) {
+        const uint32_t cap = kstart_chunk_cap(num_keys);
+        cudaError_t e = cudaMemsetAsync(chunk_count, 0, sizeof(uint32_t), s);
+        if (e != cudaSuccess) return e;
+        k_kstart_pos<<<blocks_for(n + 1u, 256), 256, 0, s>>>(sorted_key, n, kstart, num_keys, chunks, chunk_count,
+                                                             cap);
+        e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+        int dev = 0, sms = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        k_kstart_fill<<<4 * (sms > 0 ? sms : 1), 256, 0, s>>>(chunks, chunk_count, cap, kstart);
+        if (kernels) *kernels = 2;
+    } else {
+        const uint64_t warps = (entries + kKstartWindow - 1u) / kKstartWindow;
+        k_kstart<<<(unsigned)((warps + 7u) / 8u), 256, 0, s>>>(sorted_key, n, kstart, num_keys);
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_query(cudaStream_t s, uint32_t cap, const uint32_t* kstart, const uint32_t* sorted_slot,
+                         const float2* pos, const uint32_t* slot_id, TileGrid grid, uint32_t n, uint32_t* count,
+                         uint32_t* list, unsigned long long* pair_bins) {
     if (n == 0) return cudaSuccess;
     if (cap > 0 && list)
-        k_query<true><<<blocks_for(n, kQueryThreads), kQueryThreads, query_smem_bytes(cap), s>>>(
-            sorted_slot, pos, slot_id, ranges, grid, n, cap, count, list, pairs);
+        k_query<true><<<blocks_for(n, kQueryThreads), kQueryThreads, 0, s>>>(kstart, sorted_slot, pos, slot_id, grid,
+                                                                            n, cap, count, list, pair_bins);
     else
-        k_query<false><<<blocks_for(n, kQueryThreads), kQueryThreads, 0, s>>>(sorted_slot, pos, slot_id, ranges,
-                                                                             grid, n, 0u, count, nullptr, pairs);
+        k_query<false><<<blocks_for(n, kQueryThreads), kQueryThreads, 0, s>>>(kstart, sorted_slot, pos, slot_id, grid,
+                                                                             n, 0u, count, nullptr, pair_bins);
     return cudaGetLastError();
 }
 

@@ -17,6 +17,7 @@ constexpr int kMaxPasses = 3;                               // keys up to 24 bit
 constexpr int kQueryThreads = 128;
 constexpr int kStepThreads = 256;
 constexpr uint32_t kMaxCap = 256;
+constexpr uint32_t kPairBins = 256;  // pair counters (summed on read), spread to avoid one hot atomic
 
 // Entity state in slot order (structure of arrays)
 struct EntityState {
@@ -51,10 +52,17 @@ cudaError_t launch_onesweep(cudaStream_t s, const uint32_t* keys_in, const uint3
                             uint32_t* keys_out, uint32_t* vals_out, uint32_t n, uint32_t shift,
                             const uint32_t* digit_offset, uint32_t* lookback, uint32_t* ticket,
                             uint32_t* err);
-cudaError_t launch_ranges(cudaStream_t s, const uint32_t* sorted_key, uint32_t n, uint2* ranges, uint32_t num_keys);
-cudaError_t launch_query(cudaStream_t s, uint32_t cap, const uint32_t* sorted_slot, const float2* pos,
-                         const uint32_t* slot_id, const uint2* ranges, TileGrid grid, uint32_t n,
-                         uint32_t* count, uint32_t* list, unsigned long long* pairs);
+cudaError_t launch_ranges(cudaStream_t s, const uint32_t* sorted_key, uint32_t n, uint2* ranges, uint32_t num_keys,
+                          uint32_t ybits = 0);
+// Key-start table of sorted keys (num_keys + 1 entries).  chunks / chunk_count
+// (kstart_chunks(num_keys) uint4 entries and one counter; may be NULL) enable the
+// per-position kernel.  *kernels (may be NULL) receives the number of kernels launched.
+uint32_t kstart_chunks(uint64_t num_keys);
+cudaError_t launch_kstart(cudaStream_t s, const uint32_t* sorted_key, uint32_t n, uint32_t* kstart, uint32_t num_keys,
+                          uint4* chunks = nullptr, uint32_t* chunk_count = nullptr, uint32_t* kernels = nullptr);
+cudaError_t launch_query(cudaStream_t s, uint32_t cap, const uint32_t* kstart, const uint32_t* sorted_slot,
+                         const float2* pos, const uint32_t* slot_id, TileGrid grid, uint32_t n, uint32_t* count,
+                         uint32_t* list, unsigned long long* pair_bins);  // pair_bins: kPairBins counters
 cudaError_t launch_iota(cudaStream_t s, uint32_t* out, uint32_t n);
 cudaError_t launch_permute(cudaStream_t s, const uint32_t* sorted_slot, EntityState src,
                            EntityState dst, uint32_t n);

@@ -186,7 +186,10 @@ extern "C" int msim_query_neighbours_noalloc(const float* d_pos, uint32_t n, flo
     g.bits = bits;
     g.inv_cell = (float)(1.0 / cell);
     g.radius = radius;
+    g.d2_limit = sqrt_limit(radius);
     g.reach = radius;  // the query below widens it per position
+    g.ybits = 0;       // keys are tile codes only
+    g.ybands = 1.f;
     const uint32_t passes = (2 * bits + 7) / 8;
     const uint32_t sort_tiles = (n + kSortTile - 1) / kSortTile;
     const size_t keys = (size_t)1 << (2 * bits);

@@ -1,0 +1,400 @@
+// Key-start table and radius neighbour query (included by msim_kernels.cu inside
+// its namespace).
+
+// ---- key-start table ------------------------------------------------------------
+// kstart[k] = first sorted position whose key is >= k, for every k in
+// [0, num_keys]; kstart[num_keys] = n.  Keys >= num_keys (never produced by valid
+// inputs) count as num_keys - 1.  A tile's run is [kstart[t << ybits],
+// kstart[(t + 1) << ybits]); a band run inside it is two independent loads.
+constexpr uint32_t kKstartWindow = 1024;  // table entries written by one warp
+
+__device__ __forceinline__ uint32_t clamped_key(const uint32_t* __restrict__ sk, uint32_t q, uint32_t num_keys) {
+    const uint32_t k = sk[q];
+    return k < num_keys ? k : num_keys - 1u;
+}
+
+// One warp per window of kKstartWindow table entries [B, E): a 32-ary search finds
+// the first position with key >= B, then the warp walks the positions 32 at a time.
+// Position q owns the entries (key[q-1], key[q]] (clipped to the window); the
+// lanes' entry counts are laid end to end (warp prefix sum) and written 32 at a
+// time, each entry's owner found by a binary search over the prefix sums.  Every
+// warp writes exactly its window, so no warp fills a long empty stretch of the key
+// space alone.  For key spaces much smaller than n see k_kstart_search.
+__global__ __launch_bounds__(256) void k_kstart(const uint32_t* __restrict__ sk, uint32_t n,
+                                                uint32_t* __restrict__ kstart, uint32_t num_keys) {
+    constexpr uint32_t FULL = 0xffffffffu;
+    const uint32_t lane = threadIdx.x & 31;
+    const uint64_t b64 = (uint64_t)((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * kKstartWindow;
+    if (b64 > num_keys) return;  // uniform per warp
+    const uint32_t B = (uint32_t)b64;
+    const uint32_t E = (uint32_t)(b64 + kKstartWindow < (uint64_t)num_keys + 1u ? b64 + kKstartWindow
+                                                                                : (uint64_t)num_keys + 1u);
+    // first position with key >= B: the answer stays in [lo, hi], key[hi] >= B or hi = n
+    uint32_t lo = 0, hi = n;
+    while (hi - lo > 32u) {
+        const uint32_t step = (hi - lo + 31u) >> 5;
+        const uint32_t q = min(lo + (lane + 1u) * step - 1u, hi - 1u);
+        const uint32_t m = __ballot_sync(FULL, clamped_key(sk, q, num_keys) >= B);
+        if (m == 0u) {  // the last probe is hi - 1
+            lo = hi;
+            break;
+        }
+        const uint32_t f = __ffs(m) - 1u;
+        const uint32_t qf = min(lo + (f + 1u) * step - 1u, hi - 1u);
+        lo = f ? min(lo + f * step - 1u, hi - 1u) + 1u : lo;
+        hi = qf;
+    }
+    if (hi > lo) {
+        const uint32_t q = lo + lane;
+        const uint32_t m = __ballot_sync(FULL, q < hi && clamped_key(sk, q, num_keys) >= B);
+        lo = m ? lo + __ffs(m) - 1u : hi;
+    }
+    uint32_t cursor = B;  // first entry of the window not yet written
+    for (uint32_t q0 = lo; cursor < E; q0 += 32u) {
+        const uint32_t q = q0 + lane;
+        const uint32_t key = q < n ? clamped_key(sk, q, num_keys) : num_keys;  // n owns the tail up to num_keys
+        const uint32_t prev = __shfl_up_sync(FULL, key, 1);
+        const uint32_t a = lane ? prev + 1u : cursor;
+        const uint32_t b = key < E - 1u ? key : E - 1u;
+        const uint32_t len = b + 1u > a ? b + 1u - a : 0u;
+        uint32_t incl = len;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(FULL, incl, o);
+            if (lane >= (uint32_t)o) incl += y;
+        }
+        const uint32_t excl = incl - len;
+        const uint32_t total = __shfl_sync(FULL, incl, 31);
+        for (uint32_t base = 0; base < total; base += 32u) {
+            const uint32_t i = base + lane;
+            uint32_t owner = 0;  // first lane whose inclusive prefix exceeds i
+#pragma unroll
+            for (uint32_t st = 16; st > 0; st >>= 1) {
+                const uint32_t v = __shfl_sync(FULL, incl, owner + st - 1u);
+                if (v <= i) owner += st;
+            }
+            const uint32_t o_excl = __shfl_sync(FULL, excl, owner);
+            const uint32_t o_a = __shfl_sync(FULL, a, owner);
+            if (i < total) kstart[o_a + (i - o_excl)] = q0 + owner;
+        }
+        cursor = __shfl_sync(FULL, key, 31) + 1u;
+    }
+}
+
+// One thread per position q in [0, n]: q owns the entries (key[q-1], key[q]] (q = n:
+// up to num_keys).  Gaps of at most kGapDirect entries (almost all of them) are
+// written by the thread itself; gaps up to kGapWarp entries by the whole warp (the
+// lanes' gaps laid end to end, 32 coalesced entries per store); longer ones are cut
+// into chunks of kGapChunk entries, appended to a list with one atomic per warp
+// (disjoint entries, so the append order does not matter) and filled by
+// k_kstart_fill.
+constexpr uint32_t kGapDirect = 8;
+constexpr uint32_t kGapWarp = 256;
+constexpr uint32_t kGapChunk = 4096;
+
+__global__ __launch_bounds__(256) void k_kstart_pos(const uint32_t* __restrict__ sk, uint32_t n,
+                                                    uint32_t* __restrict__ kstart, uint32_t num_keys,
+                                                    uint4* __restrict__ chunks, uint32_t* chunk_count,
+                                                    uint32_t chunk_cap) {
+    constexpr uint32_t FULL = 0xffffffffu;
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
+    uint32_t from = 0, len = 0;
+    if (q <= n) {
+        from = q ? clamped_key(sk, q - 1u, num_keys) + 1u : 0u;
+        const uint32_t to = q < n ? clamped_key(sk, q, num_keys) : num_keys;  // inclusive
+        len = to >= from ? to - from + 1u : 0u;
+    }
+    if (len <= kGapDirect) {
+        for (uint32_t r = 0; r < len; r++) kstart[from + r] = q;
+    }
+    // medium gaps: the warp writes them together
+    const uint32_t wlen = len > kGapDirect && len <= kGapWarp ? len : 0u;
+    if (__any_sync(FULL, wlen != 0u)) {
+        uint32_t incl = wlen;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(FULL, incl, o);
+            if (lane >= (uint32_t)o) incl += y;
+        }
+        const uint32_t excl = incl - wlen;
+        const uint32_t total = __shfl_sync(FULL, incl, 31);
+        for (uint32_t base = 0; base < total; base += 32u) {
+            const uint32_t i = base + lane;
+            uint32_t owner = 0;
+#pragma unroll
+            for (uint32_t st = 16; st > 0; st >>= 1) {
+                const uint32_t v = __shfl_sync(FULL, incl, owner + st - 1u);
+                if (v <= i) owner += st;
+            }
+            const uint32_t o_excl = __shfl_sync(FULL, excl, owner);
+            const uint32_t o_from = __shfl_sync(FULL, from, owner);
+            const uint32_t o_q = __shfl_sync(FULL, q, owner);
+            if (i < total) kstart[o_from + (i - o_excl)] = o_q;
+        }
+    }
+    // long gaps: chunks, one list append per warp
+    const uint32_t m = len > kGapWarp ? (len + kGapChunk - 1u) / kGapChunk : 0u;
+    if (__any_sync(FULL, m != 0u)) {
+        uint32_t incl = m;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(FULL, incl, o);
+            if (lane >= (uint32_t)o) incl += y;
+        }
+        const uint32_t total = __shfl_sync(FULL, incl, 31);
+        uint32_t base = 0;
+        if (lane == 31) base = atomicAdd(chunk_count, total);
+        base = __shfl_sync(FULL, base, 31) + (incl - m);
+        if (m) {
+            if (base + m > chunk_cap) {  // unreachable: chunk_cap bounds every key space; stay correct anyway
+                for (uint32_t r = 0; r < len; r++) kstart[from + r] = q;
+            } else {
+                for (uint32_t c = 0; c < m; c++) {
+                    const uint32_t off = c * kGapChunk;
+                    chunks[base + c] = make_uint4(from + off, len - off < kGapChunk ? len - off : kGapChunk, q, 0u);
+                }
+            }
+        }
+    }
+}
+
+__global__ __launch_bounds__(256) void k_kstart_fill(const uint4* __restrict__ chunks,
+                                                     const uint32_t* __restrict__ chunk_count, uint32_t chunk_cap,
+                                                     uint32_t* __restrict__ kstart) {
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
+    const uint32_t count = min(*chunk_count, chunk_cap);
+    for (uint32_t c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; c < count; c += warps) {
+        const uint4 ch = chunks[c];
+        for (uint32_t r = lane; r < ch.y; r += 32u) kstart[ch.x + r] = ch.z;
+    }
+}
+
+// Chunk-list capacity that no key space can exceed: every chunked gap has more than
+// kGapWarp entries, and adds at most one partial chunk.
+inline uint32_t kstart_chunk_cap(uint64_t num_keys) {
+    return (uint32_t)((num_keys + 1u) / (kGapWarp + 1u) + (num_keys + 1u) / kGapChunk + 2u);
+}
+
+// One thread per table entry, binary search over the sorted keys: for key spaces
+// much smaller than the number of positions (many positions per key).
+__global__ __launch_bounds__(256) void k_kstart_search(const uint32_t* __restrict__ sk, uint32_t n,
+                                                       uint32_t* __restrict__ kstart, uint32_t num_keys) {
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k > num_keys) return;
+    uint32_t lo = 0, hi = n;  // first position with clamped key >= k
+    if (k == num_keys) {
+        lo = n;
+    } else {
+        while (lo < hi) {
+            const uint32_t mid = lo + ((hi - lo) >> 1);
+            if (clamped_key(sk, mid, num_keys) < k) lo = mid + 1u;
+            else hi = mid;
+        }
+    }
+    kstart[k] = lo;
+}
+
+// ---- radius neighbour query ------------------------------------------------------
+// A warp queries 32 consecutive sorted positions (mostly one or two tiles).  Each
+// lane's box [pos - reach, pos + reach] covers one to four tiles (more only when the
+// tile side is below 2 x reach); for every tile the lane reads the run of the y bands
+// its box overlaps from the key-start table.  The lane's runs (up to four at a time)
+// go to a shared-memory table; the warp lays all lanes' runs end to end and tests 32
+// (lane, candidate) pairs per iteration, so every lane is busy whatever the run
+// lengths.  Every candidate is tested with the predicate of random_move.comp:551-562.
+// Hits (about one per entity) update the owner's count, lower-id count and first
+// kRegKeep ids in shared memory; an entity with more than kRegKeep neighbours redoes
+// an exact pass into its output slots.  Each warp writes its lists contiguously at
+// warp * 32 * cap and adds its pair count to one of kPairBins counters; the kernel
+// has no block-wide barrier.
+// Tests every (lane, candidate) pair of the warp's runs, 32 per iteration.  The run
+// table s_base / s_end (kRuns runs per lane) is filled; flat = this lane's candidate
+// count.  Hits go to the owners' shared-memory counters and id slots.
+constexpr uint32_t kRuns = 4;  // runs per lane and round
+
+template <bool LIST>
+__device__ __forceinline__ void query_runs(uint32_t flat, uint32_t lane, uint32_t wbase, uint32_t pwarp,
+                                           const uint32_t (*s_base)[kQueryThreads],
+                                           const uint32_t (*s_end)[kQueryThreads], const float2* s_me,
+                                           const uint32_t* s_id, uint32_t* s_cnt, uint32_t (*s_keep)[kQueryThreads],
+                                           uint32_t* s_low, const uint32_t* __restrict__ sorted_slot,
+                                           const float2* __restrict__ pos, const uint32_t* __restrict__ slot_id,
+                                           const TileGrid& g, uint32_t n) {
+    constexpr uint32_t FULL = 0xffffffffu;
+    uint32_t incl = flat;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(FULL, incl, o);
+        if (lane >= (uint32_t)o) incl += y;
+    }
+    const uint32_t excl = incl - flat;
+    const uint32_t total = __shfl_sync(FULL, incl, 31);
+    __syncwarp();  // the run table is visible to the whole warp
+    for (uint32_t base = 0; base < total; base += 32u) {
+        const uint32_t i = base + lane;
+        uint32_t owner = 0;  // first lane whose inclusive prefix exceeds i
+#pragma unroll
+        for (uint32_t st = 16; st > 0; st >>= 1) {
+            const uint32_t v = __shfl_sync(FULL, incl, owner + st - 1u);
+            if (v <= i) owner += st;
+        }
+        const uint32_t o_excl = __shfl_sync(FULL, excl, owner);
+        if (i >= total) continue;
+        const uint32_t ot = wbase + owner;
+        const uint32_t r = i - o_excl;  // flat index inside the owner's runs
+        const uint32_t k =
+            (r >= s_end[0][ot] ? 1u : 0u) + (r >= s_end[1][ot] ? 1u : 0u) + (r >= s_end[2][ot] ? 1u : 0u);
+        const uint32_t q = s_base[k][ot] + r;
+        if (q == pwarp + owner) continue;  // the owner itself
+        const uint32_t s2 = sorted_slot[q];
+        if (s2 >= n) continue;
+        if (!in_range_fast(pos[s2], s_me[ot], g.radius, g.d2_limit)) continue;
+        const uint32_t oid = slot_id[s2];
+        const uint32_t c = atomicAdd(&s_cnt[ot], 1u);
+        if (LIST && c < (uint32_t)kRegKeep) s_keep[c][ot] = oid;
+        if (oid < s_id[ot]) atomicAdd(&s_low[ot], 1u);
+    }
+    __syncwarp();  // before the run table is overwritten
+}
+
+template <bool LIST>
+__global__ __launch_bounds__(kQueryThreads) void k_query(const uint32_t* __restrict__ kstart,
+                                                         const uint32_t* __restrict__ sorted_slot,
+                                                         const float2* __restrict__ pos,
+                                                         const uint32_t* __restrict__ slot_id, TileGrid g,
+                                                         uint32_t n, uint32_t cap, uint32_t* __restrict__ count_out,
+                                                         uint32_t* __restrict__ list,
+                                                         unsigned long long* __restrict__ pair_bins) {
+    constexpr uint32_t FULL = 0xffffffffu;
+    __shared__ float2 s_me[kQueryThreads];
+    __shared__ uint32_t s_id[kQueryThreads];
+    __shared__ uint32_t s_cnt[kQueryThreads];
+    __shared__ uint32_t s_low[kQueryThreads];
+    __shared__ uint32_t s_base[kRuns][kQueryThreads];  // run start position minus the lane's flat offset
+    __shared__ uint32_t s_end[kRuns][kQueryThreads];   // lane-local flat end of each run
+    __shared__ uint32_t s_keep[LIST ? kRegKeep : 1][kQueryThreads];
+    const uint32_t tid = threadIdx.x;
+    const uint32_t lane = tid & 31;
+    const uint32_t wbase = tid - lane;
+    const uint32_t p = blockIdx.x * kQueryThreads + tid;
+    const uint32_t pwarp = p - lane;
+    const bool valid = p < n;
+    float2 me = make_float2(0.f, 0.f);
+    uint32_t myid = 0;
+    uint32_t x0 = 1, x1 = 0, y0 = 1, y1 = 0;  // empty box for invalid lanes
+    float ylo = 0.f, yhi = 0.f;
+    if (valid) {
+        const uint32_t s = sorted_slot[p] < n ? sorted_slot[p] : 0u;
+        me = pos[s];
+        myid = slot_id[s];
+        ylo = __fsub_rn(me.y, g.reach);
+        yhi = __fadd_rn(me.y, g.reach);
+        x0 = tile_coord(__fsub_rn(me.x, g.reach), g.inv_cell, g.tiles_x);
+        x1 = tile_coord(__fadd_rn(me.x, g.reach), g.inv_cell, g.tiles_x);
+        y0 = tile_coord(ylo, g.inv_cell, g.tiles_y);
+        y1 = tile_coord(yhi, g.inv_cell, g.tiles_y);
+    }
+    s_me[tid] = me;
+    s_id[tid] = myid;
+    s_cnt[tid] = 0u;
+    s_low[tid] = 0u;
+    const uint32_t nx = x1 >= x0 ? x1 - x0 + 1u : 0u, ny = y1 >= y0 ? y1 - y0 + 1u : 0u;
+    if (__all_sync(FULL, nx <= 2u && ny <= 2u)) {
+        // at most 2 x 2 tiles (always when the tile side is at least 2 x reach): the
+        // tiles' Morton codes by increments; the row y0 runs from the lower box edge's
+        // band up (to the last band when the box reaches row y1), row y1 from band 0
+        const uint32_t top = (1u << g.ybits) - 1u;
+        const uint32_t b_lo = g.ybits ? y_band(g, ylo, y0) : 0u;
+        const uint32_t b_hi = g.ybits ? y_band(g, yhi, y1) : 0u;
+        const uint32_t m00 = morton2(x0, y0);
+        const uint32_t m10 = morton_inc_x(m00);
+        const uint32_t tiles[kRuns] = {m00, m10, morton_inc_y(m00), morton_inc_y(m10)};
+        const bool have[kRuns] = {nx >= 1u && ny >= 1u, nx == 2u && ny >= 1u, nx >= 1u && ny == 2u,
+                                  nx == 2u && ny == 2u};
+        uint32_t flat = 0;
+#pragma unroll
+        for (uint32_t k = 0; k < kRuns; k++) {
+            uint32_t lo = 0, len = 0;
+            if (have[k]) {
+                const uint32_t t = tiles[k] << g.ybits;
+                const uint32_t bl = k < 2u ? b_lo : 0u;
+                const uint32_t bh = k < 2u ? (ny == 2u ? top : b_hi) : b_hi;
+                lo = kstart[t | bl];
+                uint32_t hi = kstart[(t | bh) + 1u];
+                if (hi > n) hi = n;
+                len = hi > lo ? hi - lo : 0u;
+            }
+            s_base[k][tid] = lo - flat;
+            flat += len;
+            s_end[k][tid] = flat;
+        }
+        query_runs<LIST>(flat, lane, wbase, pwarp, s_base, s_end, s_me, s_id, s_cnt, s_keep, s_low, sorted_slot,
+                         pos, slot_id, g, n);
+    } else {
+        // general boxes (tile side below 2 x reach): kRuns tiles per round
+        const uint32_t nslots = nx * ny;
+        const uint32_t max_slots = __reduce_max_sync(FULL, nslots);
+#pragma unroll 1
+        for (uint32_t j0 = 0; j0 < max_slots; j0 += kRuns) {
+            uint32_t flat = 0;
+#pragma unroll 1
+            for (uint32_t k = 0; k < kRuns; k++) {
+                const uint32_t j = j0 + k;
+                uint32_t lo = 0, len = 0;
+                if (j < nslots) {
+                    const uint32_t jy = j / nx;
+                    const uint32_t tx = x0 + (j - jy * nx), ty = y0 + jy;
+                    const uint32_t t = morton2(tx, ty) << g.ybits;
+                    const uint32_t b0 = g.ybits ? y_band(g, ylo, ty) : 0u;
+                    const uint32_t b1 = g.ybits ? y_band(g, yhi, ty) : 0u;
+                    lo = kstart[t | b0];
+                    uint32_t hi = kstart[(t | b1) + 1u];
+                    if (hi > n) hi = n;
+                    len = hi > lo ? hi - lo : 0u;
+                }
+                s_base[k][tid] = lo - flat;
+                flat += len;
+                s_end[k][tid] = flat;
+            }
+            query_runs<LIST>(flat, lane, wbase, pwarp, s_base, s_end, s_me, s_id, s_cnt, s_keep, s_low,
+                             sorted_slot, pos, slot_id, g, n);
+        }
+    }
+    __syncwarp();
+    const uint32_t count = valid ? s_cnt[tid] : 0u;
+    const uint32_t lower = valid ? s_low[tid] : 0u;
+    if (valid) count_out[p] = count;
+    const uint32_t warp_lower = __reduce_add_sync(FULL, lower);
+    if (lane == 0 && warp_lower) atomicAdd(&pair_bins[(p >> 5) & (kPairBins - 1u)], (unsigned long long)warp_lower);
+    if (LIST) {
+        const uint32_t kept = count < cap ? count : cap;
+        uint32_t incl = kept;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(FULL, incl, o);
+            if (lane >= (uint32_t)o) incl += y;
+        }
+        uint32_t* out = list + (size_t)(p >> 5) * 32u * cap + (incl - kept);
+        if (count <= (uint32_t)kRegKeep) {  // every neighbour is in s_keep: sort and write
+            uint32_t keep[kRegKeep];
+#pragma unroll
+            for (int i = 0; i < kRegKeep; i++) keep[i] = (uint32_t)i < count ? s_keep[i][tid] : 0xffffffffu;
+#pragma unroll
+            for (int a = 0; a < kRegKeep; a++)
+#pragma unroll
+                for (int b = 0; b + 1 < kRegKeep - a; b++)
+                    if (keep[b] > keep[b + 1]) {
+                        const uint32_t t = keep[b];
+                        keep[b] = keep[b + 1];
+                        keep[b + 1] = t;
+                    }
+#pragma unroll
+            for (int i = 0; i < kRegKeep; i++)
+                if ((uint32_t)i < kept) out[i] = keep[i];
+        } else {
+            list_overflow(sorted_slot, pos, slot_id, kstart, g, n, p, me, x0, x1, y0, y1, cap, out);
+        }
+    }
+}

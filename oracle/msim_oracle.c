@@ -173,8 +173,9 @@ static inline uint32_t conn_at(const step_job* j, uint32_t k) {
  *   update_direction   :830-839  (d = target - pos, len = length(d), dir = d/len*SPEED)
  *   move               :841-852  (distance > SPEED ? pos + dir : snap + new_target)
  *   new_target         :778-828
- * SPEED (:750) becomes step = (speed * factor[road]) * dt; 1.4 * 1 * 1 = SPEED. */
-static void step_entity(const step_job* j, uint32_t i) {
+ * SPEED (:750) becomes step = (speed * factor[road]) * dt; 1.4 * 1 * 1 = SPEED.
+ * Returns 1 when the entity snapped to its target this tick. */
+static int step_entity(const step_job* j, uint32_t i) {
     float px = j->pos[2ull * i], py = j->pos[2ull * i + 1];
     uint32_t h = j->heading[i];
     uint32_t r = h & HEAD_ROAD;
@@ -197,7 +198,7 @@ static void step_entity(const step_job* j, uint32_t i) {
         float my = ny * step;
         j->pos[2ull * i] = px + mx;
         j->pos[2ull * i + 1] = py + my;
-        return;
+        return 0;
     }
     /* snap to the target, then new_target */
     j->pos[2ull * i] = tx;
@@ -209,14 +210,14 @@ static void step_entity(const step_job* j, uint32_t i) {
         ccnt = rc[1];
         if (ccnt <= 1) { /* U-turn toward end */
             j->heading[i] = r | HEAD_TO_END;
-            return;
+            return 1;
         }
     } else { /* :794-801 */
         cidx = rc[2];
         ccnt = rc[3];
         if (ccnt <= 1) {
             j->heading[i] = r;
-            return;
+            return 1;
         }
     }
     uint32_t nr;
@@ -233,12 +234,13 @@ static void step_entity(const step_job* j, uint32_t i) {
     } else {
         j->heading[i] = nr;
     }
+    return 1;
 }
 
 static void* step_worker(void* arg) {
     step_job* j = (step_job*)arg;
     for (uint32_t t = 0; t < j->ticks; t++)
-        for (uint32_t i = j->begin; i < j->end; i++) step_entity(j, i);
+        for (uint32_t i = j->begin; i < j->end; i++) (void)step_entity(j, i);
     return NULL;
 }
 
@@ -414,4 +416,246 @@ uint64_t oracle_neighbours(uint32_t n, const float* pos, float radius, uint32_t 
     free(start);
     free(items);
     return pairs;
+}
+
+/* ---- density calibration: FP64 adjoint reference ----------------------------- */
+
+typedef struct {
+    step_job sj;               /* map, FP32 state copies, params */
+    const float* pos0;
+    const uint32_t* head0;
+    const uint32_t* rng0;
+    double world_w, world_h;
+    uint32_t gw, gh;
+    const double* lambda;      /* phase 2: dL/dD per cell */
+    double* density;           /* phase 1: per-thread accumulator (gw*gh) */
+    double* grad_speed;        /* phase 2: per entity */
+    double* grad_factor;       /* phase 2: per-thread accumulator (num_roads) */
+    int phase;
+    int fp64_model;
+    uint32_t* sched;           /* phase 1: event bits, sched_words per entity (may be NULL) */
+    uint32_t sched_words;
+    int fbits;                 /* fraction bits of the fixed-point cell coordinates */
+} adj_job;
+
+/* Cell coordinates of position (x, y): u = x * gw / W - 1/2 (cell-centred), the
+ * lower cell index and the fraction.  For the FP32 trajectory they are computed
+ * as the forward kernel does, in binary32 with the scale rounded to binary32; for
+ * the smooth FP64 model in binary64.  *sx, *sy = du/dx, dv/dy. */
+static void cell_coords(const adj_job* a, double x, double y, long* i0, long* j0, double* fx, double* fy, double* sx,
+                        double* sy) {
+    if (a->fp64_model) {
+        *sx = (double)a->gw / a->world_w;
+        *sy = (double)a->gh / a->world_h;
+        const double u = x * *sx - 0.5, v = y * *sy - 0.5;
+        const double fi = floor(u), fj = floor(v);
+        *i0 = (long)fi;
+        *j0 = (long)fj;
+        *fx = u - fi;
+        *fy = v - fj;
+    } else {
+        /* binary32 u, then fixed point with fbits fraction bits (truncated) */
+        const float isx = (float)((double)a->gw / a->world_w), isy = (float)((double)a->gh / a->world_h);
+        const float u = (float)x * isx - 0.5f, v = (float)y * isy - 0.5f;
+        const double scale = ldexp(1.0, a->fbits), lim = ldexp(1.0, 30 - a->fbits);
+        const double U = floor(fmin(fmax((double)u, -lim), lim) * scale);
+        const double V = floor(fmin(fmax((double)v, -lim), lim) * scale);
+        const double fi = floor(U / scale), fj = floor(V / scale);
+        *sx = (double)isx;
+        *sy = (double)isy;
+        *i0 = (long)fi;
+        *j0 = (long)fj;
+        *fx = (U - fi * scale) / scale;
+        *fy = (V - fj * scale) / scale;
+    }
+}
+
+/* Bilinear, cell-centred weights of position (x, y) on the gw x gh grid over
+ * [0, W) x [0, H); corners outside the grid are dropped. */
+static void splat64(const adj_job* a, double x, double y, double w, double* grid) {
+    long i0, j0;
+    double fx, fy, sx, sy;
+    cell_coords(a, x, y, &i0, &j0, &fx, &fy, &sx, &sy);
+    double wt[4] = {(1 - fx) * (1 - fy), fx * (1 - fy), (1 - fx) * fy, fx * fy};
+    long ci[4] = {i0, i0 + 1, i0, i0 + 1}, cj[4] = {j0, j0, j0 + 1, j0 + 1};
+    for (int k = 0; k < 4; k++)
+        if (ci[k] >= 0 && ci[k] < (long)a->gw && cj[k] >= 0 && cj[k] < (long)a->gh)
+            grid[(size_t)cj[k] * a->gw + (size_t)ci[k]] += w * wt[k];
+}
+
+static double lam_at(const adj_job* a, long i, long j) {
+    if (i < 0 || j < 0 || i >= (long)a->gw || j >= (long)a->gh) return 0.0;
+    return a->lambda[(size_t)j * a->gw + (size_t)i];
+}
+
+/* d/dp of sum_g lambda_g w_g(p) */
+static void splat64_grad(const adj_job* a, double x, double y, double* gx, double* gy) {
+    long i0, j0;
+    double fx, fy, sx, sy;
+    cell_coords(a, x, y, &i0, &j0, &fx, &fy, &sx, &sy);
+    double l00 = lam_at(a, i0, j0), l10 = lam_at(a, i0 + 1, j0), l01 = lam_at(a, i0, j0 + 1),
+           l11 = lam_at(a, i0 + 1, j0 + 1);
+    *gx = ((1 - fy) * (l10 - l00) + fy * (l11 - l01)) * sx;
+    *gy = ((1 - fx) * (l01 - l00) + fx * (l11 - l10)) * sy;
+}
+
+static void* adj_worker(void* arg) {
+    adj_job* a = (adj_job*)arg;
+    step_job* j = &a->sj;
+    const uint32_t T = j->ticks;
+    double* hx = NULL;
+    double* hy = NULL;
+    uint32_t* hh = NULL;
+    unsigned char* hs = NULL;
+    if (a->phase == 2) {
+        hx = (double*)malloc(sizeof(double) * (T + 1));
+        hy = (double*)malloc(sizeof(double) * (T + 1));
+        hh = (uint32_t*)malloc(sizeof(uint32_t) * (T + 1));
+        hs = (unsigned char*)malloc(T + 1);
+    }
+    for (uint32_t i = j->begin; i < j->end; i++) {
+        j->pos[2ull * i] = a->pos0[2ull * i];
+        j->pos[2ull * i + 1] = a->pos0[2ull * i + 1];
+        j->heading[i] = a->head0[i];
+        memcpy(j->rng + 4ull * i, a->rng0 + 4ull * i, 16);
+        double x = a->pos0[2ull * i], y = a->pos0[2ull * i + 1];
+        const double s = (double)j->speed[i];
+        if (hx) {
+            hx[0] = x;
+            hy[0] = y;
+        }
+        for (uint32_t t = 1; t <= T; t++) {
+            const uint32_t h = j->heading[i];
+            /* the FP32 step: the event schedule, and the trajectory unless fp64_model */
+            const int snapped = step_entity(j, i);
+            if (!a->fp64_model) {
+                x = (double)j->pos[2ull * i];
+                y = (double)j->pos[2ull * i + 1];
+            } else {
+                const uint32_t r = h & HEAD_ROAD;
+                const float* rp = j->road_pos + 4ull * r;
+                const double tx = (h >> 31) ? rp[2] : rp[0], ty = (h >> 31) ? rp[3] : rp[1];
+                if (snapped) {
+                    x = tx;
+                    y = ty;
+                } else {
+                    const double l = s * (j->factor ? (double)j->factor[r] : 1.0) * (double)j->dt;
+                    const double dx = tx - x, dy = ty - y, L = sqrt(dx * dx + dy * dy);
+                    if (L > 0) {
+                        x += dx / L * l;
+                        y += dy / L * l;
+                    }
+                }
+            }
+            if (a->phase == 1) {
+                if (a->sched && snapped) a->sched[(size_t)i * a->sched_words + ((t - 1) >> 5)] |= 1u << ((t - 1) & 31u);
+                splat64(a, x, y, 1.0 / (double)T, a->density);
+            } else {
+                hx[t] = x;
+                hy[t] = y;
+                hh[t] = h;
+                hs[t] = (unsigned char)snapped;
+            }
+        }
+        if (a->phase == 2) { /* reverse sweep */
+            double ax = 0, ay = 0, gs = 0;
+            for (uint32_t t = T; t >= 1; t--) {
+                double gx, gy;
+                splat64_grad(a, hx[t], hy[t], &gx, &gy);
+                ax += gx / (double)T;
+                ay += gy / (double)T;
+                if (hs[t]) {
+                    ax = 0;
+                    ay = 0;
+                    continue;
+                }
+                uint32_t r = hh[t] & HEAD_ROAD;
+                const float* rp = j->road_pos + 4ull * r;
+                double tx = (hh[t] >> 31) ? rp[2] : rp[0], ty = (hh[t] >> 31) ? rp[3] : rp[1];
+                double dx = tx - hx[t - 1], dy = ty - hy[t - 1], L = sqrt(dx * dx + dy * dy);
+                if (!(L > 0)) continue;
+                double f = j->factor ? (double)j->factor[r] : 1.0;
+                double l = s * f * (double)j->dt;
+                double nx = dx / L, ny = dy / L;
+                double gl = nx * ax + ny * ay;
+                gs += gl * f * (double)j->dt;
+                a->grad_factor[r] += gl * s * (double)j->dt;
+                double k = l / L;
+                ax -= k * (ax - nx * gl);
+                ay -= k * (ay - ny * gl);
+            }
+            a->grad_speed[i] = gs;
+        }
+    }
+    free(hx);
+    free(hy);
+    free(hh);
+    free(hs);
+    return NULL;
+}
+
+double oracle_density_adjoint(uint32_t num_roads, const float* road_pos, const uint32_t* road_conn,
+                              uint32_t num_conn, const uint32_t* conn, uint32_t n, uint32_t rng_kind, float dt,
+                              uint32_t ticks, const float* pos0, const uint32_t* head0, const uint32_t* rng0,
+                              const float* speed, const float* factor, float world_w, float world_h, uint32_t gw,
+                              uint32_t gh, const float* target, double* density, double* grad_speed,
+                              double* grad_factor, int fp64_model, uint32_t* sched, int threads) {
+    if (threads <= 0) threads = 1;
+    if ((uint32_t)threads > n) threads = n ? (int)n : 1;
+    const size_t G = (size_t)gw * gh;
+    float* pos = (float*)malloc(sizeof(float) * 2 * (size_t)n + 8);
+    uint32_t* head = (uint32_t*)malloc(sizeof(uint32_t) * (size_t)n + 4);
+    uint32_t* rng = (uint32_t*)malloc(sizeof(uint32_t) * 4 * (size_t)n + 16);
+    double* dens = (double*)calloc(G * (size_t)threads, sizeof(double));
+    double* gf = (double*)calloc((size_t)num_roads * (size_t)threads, sizeof(double));
+    double* lambda = (double*)malloc(sizeof(double) * G);
+    if (sched) memset(sched, 0, sizeof(uint32_t) * (size_t)n * ((ticks + 31u) / 32u));
+    /* largest fraction bits (16..22) with |u| * 2^fbits below 2^30 on this grid */
+    int gbits = 0;
+    while ((1ull << gbits) < (uint64_t)(gw > gh ? gw : gh) + 1u) gbits++;
+    int fbits = 30 - gbits;
+    fbits = fbits > 22 ? 22 : (fbits < 16 ? 16 : fbits);
+    adj_job* jobs = (adj_job*)malloc(sizeof(adj_job) * (size_t)threads);
+    pthread_t* tids = (pthread_t*)malloc(sizeof(pthread_t) * (size_t)threads);
+    for (int phase = 1; phase <= 2; phase++) {
+        for (int t = 0; t < threads; t++) {
+            step_job sj = {num_roads, road_pos, road_conn, num_conn, conn, rng_kind, dt, factor, ticks, pos, head, rng,
+                           speed, (uint32_t)((uint64_t)n * (uint64_t)t / (uint64_t)threads),
+                           (uint32_t)((uint64_t)n * (uint64_t)(t + 1) / (uint64_t)threads)};
+            adj_job aj = {sj, pos0, head0, rng0, (double)world_w, (double)world_h, gw, gh, lambda,
+                          dens + G * (size_t)t, grad_speed, gf + (size_t)num_roads * (size_t)t, phase,
+                          fp64_model, sched, (ticks + 31u) / 32u, fbits};
+            jobs[t] = aj;
+            pthread_create(&tids[t], NULL, adj_worker, &jobs[t]);
+        }
+        for (int t = 0; t < threads; t++) pthread_join(tids[t], NULL);
+        if (phase == 1) { /* D, loss, lambda = dL/dD (thread partials summed in order) */
+            for (int t = 1; t < threads; t++)
+                for (size_t g = 0; g < G; g++) dens[g] += dens[G * (size_t)t + g];
+            for (size_t g = 0; g < G; g++) {
+                if (density) density[g] = dens[g];
+                lambda[g] = 2.0 / (double)G * (dens[g] - (double)target[g]);
+            }
+        }
+    }
+    double loss = 0;
+    for (size_t g = 0; g < G; g++) {
+        double d = dens[g] - (double)target[g];
+        loss += d * d;
+    }
+    loss /= (double)G;
+    for (uint32_t r = 0; r < num_roads; r++) {
+        double acc = 0;
+        for (int t = 0; t < threads; t++) acc += gf[(size_t)num_roads * (size_t)t + r];
+        grad_factor[r] = acc;
+    }
+    free(pos);
+    free(head);
+    free(rng);
+    free(dens);
+    free(gf);
+    free(lambda);
+    free(jobs);
+    free(tids);
+    return loss;
 }

@@ -63,6 +63,28 @@ void oracle_step(uint32_t num_roads, const float* road_pos, const uint32_t* road
 uint64_t oracle_neighbours(uint32_t n, const float* pos, float radius, uint32_t cap,
                            uint32_t* count, uint32_t* idx, int threads);
 
+/* Density calibration, FP64 reference of the loss and its gradient.  The FP32 move
+ * step (as oracle_step, from pos0/head0/rng0) gives the event schedule (ticks at
+ * which an entity snaps to its road end, and its road choices) and, unless
+ * fp64_model, the trajectory p_t; with fp64_model the trajectory follows that
+ * schedule in FP64 (p_t = p_{t-1} + (d/|d|) * speed*factor*dt, d = target -
+ * p_{t-1}; p_t = target at an event), a smooth model for finite differences.
+ * D = (1/ticks) sum_t splat(p_t) (bilinear, cell-centred, gw x gh cells over
+ * [0,W) x [0,H); for the FP32 trajectory the cell coordinate u = x*gw/W - 1/2 is
+ * formed in binary32 and truncated to fbits fraction bits, fbits the largest value
+ * in 16..22 with |u| * 2^fbits < 2^30), loss = mean_g (D_g - target_g)^2, both in
+ * FP64; the gradient is
+ * the FP64 adjoint of the step about the trajectory with the events held fixed.
+ * Writes density (may be NULL), grad_speed[n], grad_factor[num_roads] and, when
+ * sched is not NULL, the event schedule (bit t-1 of word (t-1)/32 of entity i's
+ * ceil(ticks/32) words set when i snaps at tick t); returns the loss. */
+double oracle_density_adjoint(uint32_t num_roads, const float* road_pos, const uint32_t* road_conn,
+                              uint32_t num_conn, const uint32_t* conn, uint32_t n, uint32_t rng_kind, float dt,
+                              uint32_t ticks, const float* pos0, const uint32_t* head0, const uint32_t* rng0,
+                              const float* speed, const float* factor, float world_w, float world_h, uint32_t gw,
+                              uint32_t gh, const float* target, double* density, double* grad_speed,
+                              double* grad_factor, int fp64_model, uint32_t* sched, int threads);
+
 /* The single predicate, for tests. */
 int oracle_in_range(float ax, float ay, float bx, float by, float radius);
 

@@ -169,6 +169,45 @@ def ref_lower_sets(pos, world_w, world_h, radius, node_cap=10, max_ids=256):
     return lower, events, ids
 
 
+def density_adjoint(road_map, state, speed, factor, rng_kind, dt, ticks, grid, target, threads=None,
+                    fp64_model=False, with_schedule=False):
+    """FP64 loss, density and gradients (speed, factor) of the density calibration
+    about the FP32 trajectory (or the FP64 model with the FP32 step's event
+    schedule), see msim_oracle.h; with_schedule adds the event bits (n, ceil(ticks/32))."""
+    L = lib()
+    d = ctypes.POINTER(ctypes.c_double)
+    L.oracle_density_adjoint.restype = ctypes.c_double
+    L.oracle_density_adjoint.argtypes = [ctypes.c_uint32, f32p, u32p, ctypes.c_uint32, u32p, ctypes.c_uint32,
+                                         ctypes.c_uint32, ctypes.c_float, ctypes.c_uint32, f32p, u32p, u32p, f32p,
+                                         f32p, ctypes.c_float, ctypes.c_float, ctypes.c_uint32, ctypes.c_uint32, f32p,
+                                         d, d, d, ctypes.c_int, u32p, ctypes.c_int]
+    rp = np.ascontiguousarray(road_map.road_pos, np.float32)
+    rc = np.ascontiguousarray(road_map.road_conn, np.uint32)
+    cl = np.ascontiguousarray(road_map.connections, np.uint32)
+    pos0 = np.ascontiguousarray(state["pos"], np.float32)
+    head0 = np.ascontiguousarray(state["heading"], np.uint32)
+    rng0 = np.ascontiguousarray(state["rng"], np.uint32)
+    speed = np.ascontiguousarray(speed, np.float32)
+    factor = np.ascontiguousarray(factor, np.float32)
+    target = np.ascontiguousarray(target, np.float32)
+    n = head0.shape[0]
+    G = grid[0] * grid[1]
+    dens = np.zeros(G, np.float64)
+    gs = np.zeros(n, np.float64)
+    gf = np.zeros(rp.shape[0], np.float64)
+    sched = np.zeros((n, (ticks + 31) // 32), np.uint32) if with_schedule else None
+    loss = L.oracle_density_adjoint(rp.shape[0], _p(rp, ctypes.c_float), _p(rc, ctypes.c_uint32), cl.shape[0],
+                                    _p(cl, ctypes.c_uint32), n, rng_kind, dt, ticks, _p(pos0, ctypes.c_float),
+                                    _p(head0, ctypes.c_uint32), _p(rng0, ctypes.c_uint32), _p(speed, ctypes.c_float),
+                                    _p(factor, ctypes.c_float), road_map.width, road_map.height, grid[0], grid[1],
+                                    _p(target, ctypes.c_float), _p(dens, ctypes.c_double), _p(gs, ctypes.c_double),
+                                    _p(gf, ctypes.c_double), int(bool(fp64_model)), _p(sched, ctypes.c_uint32),
+                                    threads or cpu_count())
+    if with_schedule:
+        return loss, dens, gs, gf, sched
+    return loss, dens, gs, gf
+
+
 def ref_export_tree(pos, world_w, world_h, node_cap=10):
     """The reference quad tree (max depth 8) after inserting pos in order: (nodes
     (21845, 16) uint32 words, links (n, 5) uint32 words)."""

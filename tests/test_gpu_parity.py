@@ -81,9 +81,10 @@ def test_neighbour_ticks_every_tick(msim, orc, rng_name, rng_kind, resort):
         assert cnt.sum() > 0
 
 
-@pytest.mark.parametrize("cell,passes", [(2.05, 3), (6.0, 3), (400.0, 1)])
+@pytest.mark.parametrize("cell,passes", [(2.05, 3), (6.0, 3), (400.0, 2)])
 def test_sort_pass_counts(msim, orc, cell, passes):
-    """Tile sizes that give 1 and 3 radix passes (20- to 22-bit Morton keys)."""
+    """Tile sizes that give 2 and 3 radix passes (12- to 24-bit keys: tile Morton
+    code plus up to 6 y-band bits)."""
     road_map = msim.RoadMap.lattice(64, 13)
     n, ticks = 150_000, 12
     with msim.Simulation(road_map, n, rng="pcg32", dt=0.1, radius=2.0, cap=32, cell_size=cell,
@@ -212,6 +213,40 @@ def test_crowd_beyond_cap_and_radius_boundary(msim, orc):
     assert np.array_equal(cnt, ocnt) and np.array_equal(idx, oidx)
     assert cnt[0] == 199 and np.array_equal(idx[0], np.arange(1, 65))
     assert cnt[210] == 49  # not the entities at distance exactly R
+
+
+@pytest.mark.parametrize("radius", [2.0, 0.3, 1.7, 5.55])
+def test_radius_predicate_ulp_boundary(msim, orc, radius):
+    """Pairs whose distance lies within a few ulps of R at random angles: the
+    square-root-free predicate of the query decides every pair like the oracle's
+    sqrt(dx*dx + dy*dy) < R."""
+    road_map = msim.RoadMap.lattice(64, 3)
+    rs = np.random.default_rng(int(radius * 100))
+    spacing = 8.0 * radius
+    nx = int(road_map.width // spacing) - 1
+    ny = int(road_map.height // spacing) - 1
+    pairs = min(nx * ny, 4000)
+    cells = rs.choice(nx * ny, pairs, replace=False)
+    anchor = np.stack([(cells % nx + 1) * spacing, (cells // nx + 1) * spacing], 1) + rs.uniform(0, 1, (pairs, 2))
+    anchor = anchor.astype(np.float32)
+    theta = rs.uniform(0, 2 * np.pi, pairs)
+    d = radius * (1.0 + rs.integers(-4, 5, pairs) * 2.0 ** -23)
+    partner = (anchor + np.stack([d * np.cos(theta), d * np.sin(theta)], 1)).astype(np.float32)
+    pos = np.concatenate([anchor, partner]).astype(np.float32)
+    n = pos.shape[0]
+    head = np.zeros(n, np.uint32)
+    rng = np.ones((n, 4), np.uint32)
+    speed = np.zeros(n, np.float32)
+    with msim.Simulation(road_map, n, dt=0.1, radius=radius, cap=4) as sim:
+        sim.set_entities(pos, head, rng, speed)
+        sim.step(1, neighbours=True)
+        st = sim.get_state()
+        cnt, idx = sim.get_neighbours()
+    assert np.array_equal(st["pos"].view(np.uint32), pos.view(np.uint32))
+    ocnt, oidx, _ = orc.neighbours(pos, radius, 4)
+    assert np.array_equal(cnt, ocnt) and np.array_equal(idx, oidx)
+    inside = ocnt[:pairs]
+    assert 0 < inside.sum() < pairs  # both sides of the boundary are exercised
 
 
 def test_reference_quadtree_golden(msim, golden_dir):

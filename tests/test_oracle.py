@@ -174,3 +174,57 @@ def test_oracle_matches_reference_quadtree_golden(orc, golden_dir):
         for i in range(700):
             mine = idx[i, : cnt[i]]
             assert np.array_equal(mine[mine < i], ids[i, : lower[i]])
+
+
+def _calibration_case(orc, msim, n=1500, ticks=200, side=16, grid=(64, 64), seed=5):
+    road_map = msim.RoadMap.lattice(side, seed)
+    pos, head, rng, speed = orc.init_entities(road_map.road_pos, n, 1, seed, 1, 1.0, 1.6)
+    state = {"pos": pos, "heading": head, "rng": rng}
+    hidden = np.random.default_rng(seed).uniform(0.7, 1.3, road_map.num_roads).astype(np.float32)
+    G = grid[0] * grid[1]
+    _, target, _, _ = orc.density_adjoint(road_map, state, speed, hidden, 1, 0.1, ticks, grid,
+                                          np.zeros(G, np.float32))
+    return road_map, state, speed, target.astype(np.float32)
+
+
+def test_fp64_adjoint_central_differences(orc, msim):
+    """The FP64 adjoint against central differences (step 1e-3) of the smooth FP64
+    model on 64 random parameters (32 speeds, 32 road factors) whose +-1e-3 runs
+    keep the event schedule (no road-end event crossed)."""
+    ticks, grid, h = 200, (64, 64), 1e-3
+    road_map, state, speed, target = _calibration_case(orc, msim, ticks=ticks, grid=grid)
+    factor = np.ones(road_map.num_roads, np.float32)
+
+    def run(sp, fa):
+        return orc.density_adjoint(road_map, state, sp, fa, 1, 0.1, ticks, grid, target, fp64_model=True,
+                                   with_schedule=True)
+
+    loss, _, gs, gf, sched = run(speed, factor)
+    rs = np.random.default_rng(11)
+    for kind, vec, grad in (("speed", speed, gs), ("factor", factor, gf)):
+        checked = tried = 0
+        rel = []
+        for i in rs.permutation(vec.size):
+            if checked == 32 or tried == 400:
+                break
+            tried += 1
+            res, used = [], []
+            for d in (h, -h):
+                v = vec.copy()
+                v[i] = np.float32(vec[i] + d)
+                used.append(float(v[i]))
+                out = run(v, factor) if kind == "speed" else run(speed, v)
+                if not np.array_equal(out[4], sched):
+                    break
+                res.append(out[0])
+            if len(res) < 2:
+                continue
+            fd = (res[0] - res[1]) / (used[0] - used[1])
+            # the splat is piecewise bilinear: a +-1e-3 run whose positions cross a
+            # cell-centre line sees the kink, hence the absolute term
+            err = abs(fd - grad[i])
+            assert err <= 2e-2 * abs(grad[i]) + 2e-3 * np.abs(grad).max(), (kind, i, fd, grad[i])
+            rel.append(err / max(abs(grad[i]), 1e-300))
+            checked += 1
+        assert checked == 32, (kind, checked, tried)
+        assert np.median(rel) < 1e-3, (kind, np.median(rel))
