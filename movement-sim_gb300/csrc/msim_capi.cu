@@ -633,7 +633,7 @@ int msim_get_collision_pairs(msim_ctx* c, uint64_t* pairs) {
     rc = sync_and_check(c);
     uint64_t sum = 0;
     for (uint32_t b = 0; b < kPairBins; b++) sum += h[b];
-    *pairs = sum;
+    *pairs = sum / 2u;  // the bins hold the sum of all counts: every pair from both ends
     return rc;
 }
 

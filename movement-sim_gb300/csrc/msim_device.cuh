@@ -162,7 +162,7 @@ __device__ __forceinline__ void step_entity(const DeviceMap& m, float dt, float 
 }
 
 // ---- spatial keys -------------------------------------------------------------
-__host__ __device__ __forceinline__ uint32_t part1by1(uint32_t x) {
+__host__ __device__ __forceinline__ constexpr uint32_t part1by1(uint32_t x) {
     x &= 0x0000ffffu;
     x = (x | (x << 8)) & 0x00ff00ffu;
     x = (x | (x << 4)) & 0x0f0f0f0fu;
@@ -172,6 +172,20 @@ __host__ __device__ __forceinline__ uint32_t part1by1(uint32_t x) {
 }
 __host__ __device__ __forceinline__ uint32_t morton2(uint32_t x, uint32_t y) {
     return part1by1(x) | (part1by1(y) << 1);
+}
+// Tile coordinates are below 2^11: their bit spreads come from a constant table
+// (lanes of a warp mostly share tiles, so the constant cache broadcasts).
+struct MortonTable {
+    uint32_t v[2048];
+};
+constexpr MortonTable make_morton_table() {
+    MortonTable t{};
+    for (uint32_t i = 0; i < 2048; i++) t.v[i] = part1by1(i);
+    return t;
+}
+static __constant__ MortonTable c_morton = make_morton_table();
+__device__ __forceinline__ uint32_t morton2_tile(uint32_t x, uint32_t y) {
+    return c_morton.v[x & 2047u] | (c_morton.v[y & 2047u] << 1);
 }
 // Morton code of the tile one step up in x (or y): add 1 to the interleaved x (y)
 // bits, carrying through the other axis' bits.
@@ -201,7 +215,7 @@ __device__ __forceinline__ uint32_t y_band(const TileGrid& g, float y, uint32_t 
 }
 __device__ __forceinline__ uint32_t tile_key(const TileGrid& g, float2 p) {
     const uint32_t ty = tile_coord(p.y, g.inv_cell, g.tiles_y);
-    const uint32_t t = morton2(tile_coord(p.x, g.inv_cell, g.tiles_x), ty);
+    const uint32_t t = morton2_tile(tile_coord(p.x, g.inv_cell, g.tiles_x), ty);
     return g.ybits ? ((t << g.ybits) | y_band(g, p.y, ty)) : t;
 }
 

@@ -118,6 +118,29 @@ __global__ void k_init(DeviceMap m, EntityState st, uint32_t n, uint32_t rng_kin
 // Move `ticks` ticks (state kept in registers across ticks), then optionally
 // write the tile key and accumulate the radix digit histograms of all passes.
 template <int RNG, bool KEY>
+__device__ __forceinline__ void digit_counts(uint32_t key, bool valid, uint32_t lane, uint32_t passes,
+                                             uint32_t* s_hist) {
+    // Warp-aggregated digit counts.  Slots follow the spatial order of the last
+    // re-ordering, so neighbouring lanes mostly share digits: each run of equal
+    // digits among consecutive lanes adds its length with one shared atomic, issued
+    // by the run's first lane (found by ballot).
+    const unsigned vm = __ballot_sync(0xffffffffu, valid);
+    for (uint32_t ps = 0; ps < passes; ps++) {
+        const uint32_t d = (key >> (8u * ps)) & 0xffu;
+        const uint32_t dprev = __shfl_up_sync(0xffffffffu, d, 1);
+        const bool head = valid && (lane == 0 || d != dprev);
+        const unsigned heads = __ballot_sync(0xffffffffu, head);
+        if (head) {
+            const unsigned later = heads & ~((2u << lane) - 1u);  // heads after this lane
+            const uint32_t end = later ? (uint32_t)(__ffs(later) - 1) : (uint32_t)(32 - __clz(vm));
+            atomicAdd(&s_hist[ps * kRadix + d], end - lane);
+        }
+    }
+}
+
+// Two entities per thread and iteration (slots s and s + stride): both entities'
+// loads are in flight before either is stepped.
+template <int RNG, bool KEY>
 __global__ __launch_bounds__(kStepThreads) void k_step(StepLaunch a) {
     __shared__ uint32_t s_hist[kMaxPasses * kRadix];
     if (KEY) {
@@ -126,46 +149,48 @@ __global__ __launch_bounds__(kStepThreads) void k_step(StepLaunch a) {
     }
     const uint32_t lane = threadIdx.x & 31;
     const uint32_t stride = gridDim.x * kStepThreads;
-    for (uint32_t base = blockIdx.x * kStepThreads; base < a.n; base += stride) {
-        const uint32_t s = base + threadIdx.x;
-        const bool valid = s < a.n;
-        uint32_t key = 0u;
-        if (valid) {
-            float2 p = a.st.pos[s];
+    for (uint32_t base = blockIdx.x * kStepThreads; base < a.n; base += 2u * stride) {
+        uint32_t sl[2];
+        bool valid[2];
+        float2 p[2];
+        uint32_t h[2], h0[2];
+        float sp[2];
+#pragma unroll
+        for (int u = 0; u < 2; u++) {
+            sl[u] = base + u * stride + threadIdx.x;
+            valid[u] = sl[u] < a.n;
+            p[u] = make_float2(0.f, 0.f);
+            h[u] = h0[u] = 0u;
+            sp[u] = 0.f;
+            if (valid[u]) {
+                p[u] = a.st.pos[sl[u]];
+                if (a.ticks) {
+                    h[u] = h0[u] = a.st.head[sl[u]];
+                    sp[u] = a.st.speed[sl[u]];
+                }
+            }
+        }
+        uint32_t key[2] = {0u, 0u};
+#pragma unroll
+        for (int u = 0; u < 2; u++) {
+            if (!valid[u]) continue;
             if (a.ticks) {
-                uint32_t h = a.st.head[s];
-                const uint32_t h0 = h;
-                const float sp = a.st.speed[s];
                 uint4 r = make_uint4(0u, 0u, 0u, 0u);
                 bool rl = false, rd = false;
                 for (uint32_t t = 0; t < a.ticks; t++)
-                    step_entity<RNG>(a.map, a.dt, sp, p, h, r, rl, rd, a.st.rng + s, a.err);
-                a.st.pos[s] = p;
-                if (h != h0) a.st.head[s] = h;
-                if (rd) a.st.rng[s] = r;
+                    step_entity<RNG>(a.map, a.dt, sp[u], p[u], h[u], r, rl, rd, a.st.rng + sl[u], a.err);
+                a.st.pos[sl[u]] = p[u];
+                if (h[u] != h0[u]) a.st.head[sl[u]] = h[u];
+                if (rd) a.st.rng[sl[u]] = r;
             }
             if (KEY) {
-                key = tile_key(a.grid, p);
-                a.key[s] = key;
+                key[u] = tile_key(a.grid, p[u]);
+                a.key[sl[u]] = key[u];
             }
         }
         if (KEY) {
-            // Warp-aggregated digit counts.  Slots follow the spatial order of the
-            // last re-ordering, so neighbouring lanes mostly share digits: each run
-            // of equal digits among consecutive lanes adds its length with one
-            // shared atomic, issued by the run's first lane (found by ballot).
-            const unsigned vm = __ballot_sync(0xffffffffu, valid);
-            for (uint32_t ps = 0; ps < a.passes; ps++) {
-                const uint32_t d = (key >> (8u * ps)) & 0xffu;
-                const uint32_t dprev = __shfl_up_sync(0xffffffffu, d, 1);
-                const bool head = valid && (lane == 0 || d != dprev);
-                const unsigned heads = __ballot_sync(0xffffffffu, head);
-                if (head) {
-                    const unsigned later = heads & ~((2u << lane) - 1u);  // heads after this lane
-                    const uint32_t end = later ? (uint32_t)(__ffs(later) - 1) : (uint32_t)(32 - __clz(vm));
-                    atomicAdd(&s_hist[ps * kRadix + d], end - lane);
-                }
-            }
+            digit_counts<RNG, KEY>(key[0], valid[0], lane, a.passes, s_hist);
+            digit_counts<RNG, KEY>(key[1], valid[1], lane, a.passes, s_hist);
         }
     }
     if (KEY) {
@@ -190,13 +215,24 @@ __global__ __launch_bounds__(kRadix) void k_hist_scan(const uint32_t* hist, uint
 // rank their 4096 items with warp-level multi-split (__match_any_sync) into
 // per-warp digit counters, publish per-digit counts and resolve their global
 // offsets by looking back over earlier tiles.  Every wait is bounded.
-__global__ __launch_bounds__(kSortThreads) void k_onesweep(const uint32_t* __restrict__ keys_in,
-                                                           const uint32_t* __restrict__ vals_in,
-                                                           uint32_t* __restrict__ keys_out,
-                                                           uint32_t* __restrict__ vals_out, uint32_t n,
-                                                           uint32_t shift, const uint32_t* __restrict__ digit_offset,
-                                                           uint32_t* lookback, uint32_t* ticket, uint32_t* err) {
+//
+// Ranking runs in three sweeps over the rows so that no row waits for the
+// previous one: (1) match every row's digits (group size, leader lane, rank inside
+// the row); (2) each group's leader adds the group size to the warp's counter for
+// its digit with an atomic that returns the previous count - a warp's shared-memory
+// atomics take effect in issue order, i.e. in row order, which keeps the pass
+// stable; (3) the previous counts are broadcast from the leaders (steps 2 and 3
+// four rows at a time).  Values are read
+// only for the local scatter, so they hold no registers during the ranking.
+__global__ __launch_bounds__(kSortThreads, 4) void k_onesweep(const uint32_t* __restrict__ keys_in,
+                                                              const uint32_t* __restrict__ vals_in,
+                                                              uint32_t* __restrict__ keys_out,
+                                                              uint32_t* __restrict__ vals_out, uint32_t n,
+                                                              uint32_t shift,
+                                                              const uint32_t* __restrict__ digit_offset,
+                                                              uint32_t* lookback, uint32_t* ticket, uint32_t* err) {
     constexpr int NW = kSortThreads / 32;
+    constexpr uint32_t FULL = 0xffffffffu;
     __shared__ uint32_t s_keys[kSortTile];
     __shared__ uint32_t s_vals[kSortTile];
     __shared__ uint32_t s_whist[NW * kRadix];  // per-warp counts, then exclusive warp prefix
@@ -211,33 +247,48 @@ __global__ __launch_bounds__(kSortThreads) void k_onesweep(const uint32_t* __res
     __syncthreads();
     const uint32_t tile = s_tile;
     const uint32_t base = tile * kSortTile;
+    const uint32_t row0 = base + warp * (kSortRows * 32) + lane;
 
-    uint32_t k[kSortRows], v[kSortRows], rk[kSortRows];
+    uint32_t k[kSortRows], rk[kSortRows];
 #pragma unroll
     for (int r = 0; r < kSortRows; r++) {
-        const uint32_t idx = base + warp * (kSortRows * 32) + r * 32 + lane;
-        const bool ok = idx < n;
-        k[r] = ok ? keys_in[idx] : 0u;
-        v[r] = ok ? (vals_in ? vals_in[idx] : idx) : 0u;
-        rk[r] = 0u;
+        const uint32_t idx = row0 + r * 32;
+        k[r] = idx < n ? keys_in[idx] : 0u;
     }
-    // warp-level multi-split ranking, rows in order -> stable
     uint32_t* wh = s_whist + warp * kRadix;
     const uint32_t lt = lanemask_lt();
+    // (1) per row: rank inside the row | leader lane << 8 | group size << 16
 #pragma unroll
     for (int r = 0; r < kSortRows; r++) {
-        const uint32_t idx = base + warp * (kSortRows * 32) + r * 32 + lane;
+        const uint32_t idx = row0 + r * 32;
         const bool ok = idx < n;
-        const unsigned vm = __ballot_sync(0xffffffffu, ok);
+        const unsigned vm = __ballot_sync(FULL, ok);
+        rk[r] = 0u;
         if (ok) {
-            const uint32_t d = (k[r] >> shift) & 0xffu;
-            const unsigned peers = __match_any_sync(vm, d);
-            const uint32_t cnt = wh[d];
-            rk[r] = cnt + (uint32_t)__popc(peers & lt);
-            __syncwarp(vm);
-            if ((int)lane == __ffs(peers) - 1) wh[d] = cnt + (uint32_t)__popc(peers);
+            const unsigned peers = __match_any_sync(vm, (k[r] >> shift) & 0xffu);
+            rk[r] = (uint32_t)__popc(peers & lt) | ((uint32_t)(__ffs(peers) - 1) << 8) |
+                    ((uint32_t)__popc(peers) << 16);
         }
-        __syncwarp();
+    }
+    // (2) leaders take their group's counts, in row order, four rows in flight;
+    // (3) broadcast from the leaders
+#pragma unroll
+    for (int r0 = 0; r0 < kSortRows; r0 += 4) {
+        uint32_t old[4];
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            const int r = r0 + q;
+            old[q] = 0u;
+            const uint32_t idx = row0 + r * 32;
+            if (idx < n && ((rk[r] >> 8) & 0xffu) == lane)
+                old[q] = atomicAdd(&wh[(k[r] >> shift) & 0xffu], rk[r] >> 16);
+        }
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            const int r = r0 + q;
+            const uint32_t from_leader = __shfl_sync(FULL, old[q], (rk[r] >> 8) & 0x1fu);
+            rk[r] = from_leader + (rk[r] & 0xffu);
+        }
     }
     __syncthreads();
 
@@ -254,21 +305,33 @@ __global__ __launch_bounds__(kSortThreads) void k_onesweep(const uint32_t* __res
     st_relaxed(my_lb, (tile == 0 ? kFlagPrefix : kFlagAgg) | tot);
     uint32_t excl = 0u;
     if (tile > 0) {
+        // look back four tiles per round of loads
         int32_t j = (int32_t)tile - 1;
         uint32_t spins = 0u;
-        while (j >= 0) {
-            const uint32_t w = ld_relaxed(lookback + (size_t)j * kRadix + d);
-            if ((w & kFlagMask) == 0u) {
+        bool done = false;
+        while (!done) {
+            uint32_t w[4];
+#pragma unroll
+            for (int q = 0; q < 4; q++)
+                w[q] = j - q >= 0 ? ld_relaxed(lookback + (size_t)(j - q) * kRadix + d) : kFlagPrefix;
+            int q = 0;
+            for (; q < 4; q++) {
+                if ((w[q] & kFlagMask) == 0u) break;  // not published yet: poll it again
+                excl += w[q] & kValueMask;
+                if (w[q] & kFlagPrefix) {
+                    done = true;
+                    break;
+                }
+            }
+            if (done) break;
+            j -= q;
+            if (q < 4) {
                 if (++spins > kSpinLimit) {
                     atomicOr(err, kErrTimeout);
                     break;
                 }
                 __nanosleep(32);
-                continue;
             }
-            excl += w & kValueMask;
-            if (w & kFlagPrefix) break;
-            j--;
         }
         st_relaxed(my_lb, kFlagPrefix | ((excl + tot) & kValueMask));
     }
@@ -278,9 +341,15 @@ __global__ __launch_bounds__(kSortThreads) void k_onesweep(const uint32_t* __res
     __syncthreads();  // every thread reads other digits' starts below
 
     // local scatter into shared memory (digit-major), then coalesced runs out
+    uint32_t v[kSortRows];
 #pragma unroll
     for (int r = 0; r < kSortRows; r++) {
-        const uint32_t idx = base + warp * (kSortRows * 32) + r * 32 + lane;
+        const uint32_t idx = row0 + r * 32;
+        v[r] = idx < n ? (vals_in ? vals_in[idx] : idx) : 0u;
+    }
+#pragma unroll
+    for (int r = 0; r < kSortRows; r++) {
+        const uint32_t idx = row0 + r * 32;
         if (idx < n) {
             const uint32_t dd = (k[r] >> shift) & 0xffu;
             const uint32_t lpos = s_local_start[dd] + s_whist[warp * kRadix + dd] + rk[r];
@@ -294,7 +363,10 @@ __global__ __launch_bounds__(kSortThreads) void k_onesweep(const uint32_t* __res
     }
     __syncthreads();
     const uint32_t count = (n - base) < kSortTile ? (n - base) : kSortTile;
-    for (uint32_t i = tid; i < count; i += kSortThreads) {
+#pragma unroll
+    for (int r = 0; r < kSortRows; r++) {  // independent rows: their shared loads overlap
+        const uint32_t i = tid + r * kSortThreads;
+        if (i >= count) continue;
         const uint32_t key = s_keys[i];
         const uint32_t dd = (key >> shift) & 0xffu;
         const uint32_t g = s_global_base[dd] + (i - s_local_start[dd]);
@@ -536,6 +608,12 @@ cudaError_t launch_onesweep(cudaStream_t s, const uint32_t* keys_in, const uint3
                             uint32_t* vals_out, uint32_t n, uint32_t shift, const uint32_t* digit_offset,
                             uint32_t* lookback, uint32_t* ticket, uint32_t* err) {
     if (n == 0) return cudaSuccess;
+    static bool carveout = false;  // prefer the largest shared-memory carveout: 4 blocks of 43 KB per SM
+    if (!carveout) {
+        cudaFuncSetAttribute(k_onesweep, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
+        cudaGetLastError();
+        carveout = true;
+    }
     k_onesweep<<<blocks_for(n, kSortTile), kSortThreads, 0, s>>>(keys_in, vals_in, keys_out, vals_out, n, shift,
                                                                  digit_offset, lookback, ticket, err);
     return cudaGetLastError();
@@ -583,6 +661,15 @@ cudaError_t launch_query(cudaStream_t s, uint32_t cap, const uint32_t* kstart, c
                          const float2* pos, const uint32_t* slot_id, TileGrid grid, uint32_t n, uint32_t* count,
                          uint32_t* list, unsigned long long* pair_bins) {
     if (n == 0) return cudaSuccess;
+    static bool carveout = false;  // 16 blocks of ~9.5 KB per SM
+    if (!carveout) {
+        cudaFuncSetAttribute(k_query<true>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                             cudaSharedmemCarveoutMaxShared);
+        cudaFuncSetAttribute(k_query<false>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                             cudaSharedmemCarveoutMaxShared);
+        cudaGetLastError();
+        carveout = true;
+    }
     if (cap > 0 && list)
         k_query<true><<<blocks_for(n, kQueryThreads), kQueryThreads, 0, s>>>(kstart, sorted_slot, pos, slot_id, grid,
                                                                             n, cap, count, list, pair_bins);

@@ -200,63 +200,87 @@ __global__ __launch_bounds__(256) void k_kstart_search(const uint32_t* __restric
 // A warp queries 32 consecutive sorted positions (mostly one or two tiles).  Each
 // lane's box [pos - reach, pos + reach] covers one to four tiles (more only when the
 // tile side is below 2 x reach); for every tile the lane reads the run of the y bands
-// its box overlaps from the key-start table.  The lane's runs (up to four at a time)
-// go to a shared-memory table; the warp lays all lanes' runs end to end and tests 32
-// (lane, candidate) pairs per iteration, so every lane is busy whatever the run
-// lengths.  Every candidate is tested with the predicate of random_move.comp:551-562.
-// Hits (about one per entity) update the owner's count, lower-id count and first
-// kRegKeep ids in shared memory; an entity with more than kRegKeep neighbours redoes
-// an exact pass into its output slots.  Each warp writes its lists contiguously at
-// warp * 32 * cap and adds its pair count to one of kPairBins counters; the kernel
-// has no block-wide barrier.
-// Tests every (lane, candidate) pair of the warp's runs, 32 per iteration.  The run
-// table s_base / s_end (kRuns runs per lane) is filled; flat = this lane's candidate
-// count.  Hits go to the owners' shared-memory counters and id slots.
-constexpr uint32_t kRuns = 4;  // runs per lane and round
+// its box overlaps from the key-start table.  The warp lays all non-empty runs of its
+// lanes end to end in a shared run list (flat start, start position, owner lane) and
+// tests 32 (owner, candidate) pairs per iteration, so every lane is busy whatever the
+// run lengths; the run of each pair comes from a bit mask of the runs that start in
+// the current window of 32 pairs.  Every candidate is tested with the predicate of
+// random_move.comp:551-562.  A hit adds one to the owner's count and, for the first
+// kRegKeep hits, keeps the candidate's slot; ids are looked up only for those.  An
+// entity with more than kRegKeep neighbours redoes an exact pass into its output
+// slots.  The predicate is symmetric (fl(a - b) = -fl(b - a)), so the pair count is
+// half the sum of the counts.  Each warp writes its lists contiguously at
+// warp * 32 * cap and adds its count sum to one of kPairBins counters; the kernel has
+// no block-wide barrier.
+constexpr uint32_t kRuns = 4;                  // runs per lane and round
+constexpr uint32_t kWarpRuns = 32u * kRuns;    // run-list capacity of a warp
+
+struct QueryShared {
+    float2 me[kQueryThreads];
+    uint32_t cnt[kQueryThreads];
+    uint32_t keep[kRegKeep][kQueryThreads];    // slots of the first kRegKeep hits
+    uint32_t rq[kQueryThreads / 32][kWarpRuns];   // run start position minus its flat start
+    uint32_t rfs[kQueryThreads / 32][kWarpRuns];  // flat start of the run
+    uint32_t rown[kQueryThreads / 32][kWarpRuns]; // owner lane
+};
 
 template <bool LIST>
-__device__ __forceinline__ void query_runs(uint32_t flat, uint32_t lane, uint32_t wbase, uint32_t pwarp,
-                                           const uint32_t (*s_base)[kQueryThreads],
-                                           const uint32_t (*s_end)[kQueryThreads], const float2* s_me,
-                                           const uint32_t* s_id, uint32_t* s_cnt, uint32_t (*s_keep)[kQueryThreads],
-                                           uint32_t* s_low, const uint32_t* __restrict__ sorted_slot,
-                                           const float2* __restrict__ pos, const uint32_t* __restrict__ slot_id,
+__device__ __forceinline__ void query_runs(const uint32_t (&lo)[kRuns], const uint32_t (&len)[kRuns], uint32_t lane,
+                                           uint32_t warp, uint32_t pwarp, QueryShared& sh,
+                                           const uint32_t* __restrict__ sorted_slot, const float2* __restrict__ pos,
                                            const TileGrid& g, uint32_t n) {
     constexpr uint32_t FULL = 0xffffffffu;
-    uint32_t incl = flat;
+    uint32_t flat = 0, nr = 0;
+#pragma unroll
+    for (uint32_t k = 0; k < kRuns; k++) {
+        flat += len[k];
+        nr += len[k] ? 1u : 0u;
+    }
+    uint32_t fi = flat, ri = nr;  // inclusive warp prefixes of candidates and runs
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
-        const uint32_t y = __shfl_up_sync(FULL, incl, o);
-        if (lane >= (uint32_t)o) incl += y;
-    }
-    const uint32_t excl = incl - flat;
-    const uint32_t total = __shfl_sync(FULL, incl, 31);
-    __syncwarp();  // the run table is visible to the whole warp
-    for (uint32_t base = 0; base < total; base += 32u) {
-        const uint32_t i = base + lane;
-        uint32_t owner = 0;  // first lane whose inclusive prefix exceeds i
-#pragma unroll
-        for (uint32_t st = 16; st > 0; st >>= 1) {
-            const uint32_t v = __shfl_sync(FULL, incl, owner + st - 1u);
-            if (v <= i) owner += st;
+        const uint32_t yf = __shfl_up_sync(FULL, fi, o);
+        const uint32_t yr = __shfl_up_sync(FULL, ri, o);
+        if (lane >= (uint32_t)o) {
+            fi += yf;
+            ri += yr;
         }
-        const uint32_t o_excl = __shfl_sync(FULL, excl, owner);
+    }
+    const uint32_t total = __shfl_sync(FULL, fi, 31);
+    const uint32_t runs = __shfl_sync(FULL, ri, 31);
+    uint32_t j = ri - nr, fs = fi - flat;
+#pragma unroll
+    for (uint32_t k = 0; k < kRuns; k++) {
+        if (len[k]) {
+            sh.rq[warp][j] = lo[k] - fs;
+            sh.rfs[warp][j] = fs;
+            sh.rown[warp][j] = lane;
+            j++;
+            fs += len[k];
+        }
+    }
+    __syncwarp();  // the run list is visible to the whole warp
+    uint32_t ra = 0;  // first run that starts at or after the current window
+    for (uint32_t base = 0; base < total; base += 32u) {
+        const uint32_t rr = ra + lane;
+        const uint32_t off = (rr < runs ? sh.rfs[warp][rr] : 0xffffffffu) - base;
+        const uint32_t marks = __reduce_or_sync(FULL, off < 32u ? (1u << off) : 0u);
+        const uint32_t le = marks & (0xffffffffu >> (31u - lane));
+        const uint32_t run = ra + (uint32_t)__popc(le) - 1u;  // le == 0: the run begun before the window
+        ra += (uint32_t)__popc(marks);
+        const uint32_t i = base + lane;
         if (i >= total) continue;
-        const uint32_t ot = wbase + owner;
-        const uint32_t r = i - o_excl;  // flat index inside the owner's runs
-        const uint32_t k =
-            (r >= s_end[0][ot] ? 1u : 0u) + (r >= s_end[1][ot] ? 1u : 0u) + (r >= s_end[2][ot] ? 1u : 0u);
-        const uint32_t q = s_base[k][ot] + r;
+        const uint32_t q = sh.rq[warp][run] + i;
+        const uint32_t owner = sh.rown[warp][run];
         if (q == pwarp + owner) continue;  // the owner itself
         const uint32_t s2 = sorted_slot[q];
         if (s2 >= n) continue;
-        if (!in_range_fast(pos[s2], s_me[ot], g.radius, g.d2_limit)) continue;
-        const uint32_t oid = slot_id[s2];
-        const uint32_t c = atomicAdd(&s_cnt[ot], 1u);
-        if (LIST && c < (uint32_t)kRegKeep) s_keep[c][ot] = oid;
-        if (oid < s_id[ot]) atomicAdd(&s_low[ot], 1u);
+        const uint32_t ot = warp * 32u + owner;
+        if (!in_range_fast(pos[s2], sh.me[ot], g.radius, g.d2_limit)) continue;
+        const uint32_t c = atomicAdd(&sh.cnt[ot], 1u);
+        if (LIST && c < (uint32_t)kRegKeep) sh.keep[c][ot] = s2;
     }
-    __syncwarp();  // before the run table is overwritten
+    __syncwarp();  // before the run list is rewritten
 }
 
 template <bool LIST>
@@ -268,27 +292,19 @@ __global__ __launch_bounds__(kQueryThreads) void k_query(const uint32_t* __restr
                                                          uint32_t* __restrict__ list,
                                                          unsigned long long* __restrict__ pair_bins) {
     constexpr uint32_t FULL = 0xffffffffu;
-    __shared__ float2 s_me[kQueryThreads];
-    __shared__ uint32_t s_id[kQueryThreads];
-    __shared__ uint32_t s_cnt[kQueryThreads];
-    __shared__ uint32_t s_low[kQueryThreads];
-    __shared__ uint32_t s_base[kRuns][kQueryThreads];  // run start position minus the lane's flat offset
-    __shared__ uint32_t s_end[kRuns][kQueryThreads];   // lane-local flat end of each run
-    __shared__ uint32_t s_keep[LIST ? kRegKeep : 1][kQueryThreads];
+    __shared__ QueryShared sh;
     const uint32_t tid = threadIdx.x;
     const uint32_t lane = tid & 31;
-    const uint32_t wbase = tid - lane;
+    const uint32_t warp = tid >> 5;
     const uint32_t p = blockIdx.x * kQueryThreads + tid;
     const uint32_t pwarp = p - lane;
     const bool valid = p < n;
     float2 me = make_float2(0.f, 0.f);
-    uint32_t myid = 0;
     uint32_t x0 = 1, x1 = 0, y0 = 1, y1 = 0;  // empty box for invalid lanes
     float ylo = 0.f, yhi = 0.f;
     if (valid) {
         const uint32_t s = sorted_slot[p] < n ? sorted_slot[p] : 0u;
         me = pos[s];
-        myid = slot_id[s];
         ylo = __fsub_rn(me.y, g.reach);
         yhi = __fadd_rn(me.y, g.reach);
         x0 = tile_coord(__fsub_rn(me.x, g.reach), g.inv_cell, g.tiles_x);
@@ -296,10 +312,8 @@ __global__ __launch_bounds__(kQueryThreads) void k_query(const uint32_t* __restr
         y0 = tile_coord(ylo, g.inv_cell, g.tiles_y);
         y1 = tile_coord(yhi, g.inv_cell, g.tiles_y);
     }
-    s_me[tid] = me;
-    s_id[tid] = myid;
-    s_cnt[tid] = 0u;
-    s_low[tid] = 0u;
+    sh.me[tid] = me;
+    sh.cnt[tid] = 0u;
     const uint32_t nx = x1 >= x0 ? x1 - x0 + 1u : 0u, ny = y1 >= y0 ? y1 - y0 + 1u : 0u;
     if (__all_sync(FULL, nx <= 2u && ny <= 2u)) {
         // at most 2 x 2 tiles (always when the tile side is at least 2 x reach): the
@@ -308,66 +322,59 @@ __global__ __launch_bounds__(kQueryThreads) void k_query(const uint32_t* __restr
         const uint32_t top = (1u << g.ybits) - 1u;
         const uint32_t b_lo = g.ybits ? y_band(g, ylo, y0) : 0u;
         const uint32_t b_hi = g.ybits ? y_band(g, yhi, y1) : 0u;
-        const uint32_t m00 = morton2(x0, y0);
+        const uint32_t m00 = morton2_tile(x0, y0);
         const uint32_t m10 = morton_inc_x(m00);
         const uint32_t tiles[kRuns] = {m00, m10, morton_inc_y(m00), morton_inc_y(m10)};
         const bool have[kRuns] = {nx >= 1u && ny >= 1u, nx == 2u && ny >= 1u, nx >= 1u && ny == 2u,
                                   nx == 2u && ny == 2u};
-        uint32_t flat = 0;
+        uint32_t lo[kRuns], len[kRuns];
 #pragma unroll
         for (uint32_t k = 0; k < kRuns; k++) {
-            uint32_t lo = 0, len = 0;
-            if (have[k]) {
+            lo[k] = 0u;
+            len[k] = 0u;
+            if (__any_sync(FULL, have[k]) && have[k]) {
                 const uint32_t t = tiles[k] << g.ybits;
                 const uint32_t bl = k < 2u ? b_lo : 0u;
                 const uint32_t bh = k < 2u ? (ny == 2u ? top : b_hi) : b_hi;
-                lo = kstart[t | bl];
+                lo[k] = kstart[t | bl];
                 uint32_t hi = kstart[(t | bh) + 1u];
                 if (hi > n) hi = n;
-                len = hi > lo ? hi - lo : 0u;
+                len[k] = hi > lo[k] ? hi - lo[k] : 0u;
             }
-            s_base[k][tid] = lo - flat;
-            flat += len;
-            s_end[k][tid] = flat;
         }
-        query_runs<LIST>(flat, lane, wbase, pwarp, s_base, s_end, s_me, s_id, s_cnt, s_keep, s_low, sorted_slot,
-                         pos, slot_id, g, n);
+        query_runs<LIST>(lo, len, lane, warp, pwarp, sh, sorted_slot, pos, g, n);
     } else {
         // general boxes (tile side below 2 x reach): kRuns tiles per round
         const uint32_t nslots = nx * ny;
         const uint32_t max_slots = __reduce_max_sync(FULL, nslots);
 #pragma unroll 1
         for (uint32_t j0 = 0; j0 < max_slots; j0 += kRuns) {
-            uint32_t flat = 0;
-#pragma unroll 1
+            uint32_t lo[kRuns], len[kRuns];
+#pragma unroll
             for (uint32_t k = 0; k < kRuns; k++) {
                 const uint32_t j = j0 + k;
-                uint32_t lo = 0, len = 0;
+                lo[k] = 0u;
+                len[k] = 0u;
                 if (j < nslots) {
                     const uint32_t jy = j / nx;
                     const uint32_t tx = x0 + (j - jy * nx), ty = y0 + jy;
                     const uint32_t t = morton2(tx, ty) << g.ybits;
                     const uint32_t b0 = g.ybits ? y_band(g, ylo, ty) : 0u;
                     const uint32_t b1 = g.ybits ? y_band(g, yhi, ty) : 0u;
-                    lo = kstart[t | b0];
+                    lo[k] = kstart[t | b0];
                     uint32_t hi = kstart[(t | b1) + 1u];
                     if (hi > n) hi = n;
-                    len = hi > lo ? hi - lo : 0u;
+                    len[k] = hi > lo[k] ? hi - lo[k] : 0u;
                 }
-                s_base[k][tid] = lo - flat;
-                flat += len;
-                s_end[k][tid] = flat;
             }
-            query_runs<LIST>(flat, lane, wbase, pwarp, s_base, s_end, s_me, s_id, s_cnt, s_keep, s_low,
-                             sorted_slot, pos, slot_id, g, n);
+            query_runs<LIST>(lo, len, lane, warp, pwarp, sh, sorted_slot, pos, g, n);
         }
     }
     __syncwarp();
-    const uint32_t count = valid ? s_cnt[tid] : 0u;
-    const uint32_t lower = valid ? s_low[tid] : 0u;
+    const uint32_t count = valid ? sh.cnt[tid] : 0u;
     if (valid) count_out[p] = count;
-    const uint32_t warp_lower = __reduce_add_sync(FULL, lower);
-    if (lane == 0 && warp_lower) atomicAdd(&pair_bins[(p >> 5) & (kPairBins - 1u)], (unsigned long long)warp_lower);
+    const uint32_t warp_sum = __reduce_add_sync(FULL, count);  // every pair is seen from both ends
+    if (lane == 0 && warp_sum) atomicAdd(&pair_bins[(p >> 5) & (kPairBins - 1u)], (unsigned long long)warp_sum);
     if (LIST) {
         const uint32_t kept = count < cap ? count : cap;
         uint32_t incl = kept;
@@ -377,10 +384,10 @@ __global__ __launch_bounds__(kQueryThreads) void k_query(const uint32_t* __restr
             if (lane >= (uint32_t)o) incl += y;
         }
         uint32_t* out = list + (size_t)(p >> 5) * 32u * cap + (incl - kept);
-        if (count <= (uint32_t)kRegKeep) {  // every neighbour is in s_keep: sort and write
+        if (count <= (uint32_t)kRegKeep) {  // every neighbour is kept: ids, sort, write
             uint32_t keep[kRegKeep];
 #pragma unroll
-            for (int i = 0; i < kRegKeep; i++) keep[i] = (uint32_t)i < count ? s_keep[i][tid] : 0xffffffffu;
+            for (int i = 0; i < kRegKeep; i++) keep[i] = (uint32_t)i < count ? slot_id[sh.keep[i][tid]] : 0xffffffffu;
 #pragma unroll
             for (int a = 0; a < kRegKeep; a++)
 #pragma unroll
