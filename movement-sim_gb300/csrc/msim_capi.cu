@@ -65,6 +65,7 @@ struct msim_ctx {
     uint32_t* tickets = nullptr;
     uint32_t* kstart = nullptr;  // first sorted position of every key, 2^key_bits + 1 entries
     uint4* kstart_chunks = nullptr;  // long key gaps, filled by a second kernel
+    float2* sorted_pos = nullptr;    // positions in sorted order (the query's candidates)
     uint32_t* kstart_chunk_count = nullptr;
     size_t num_keys = 0;
     uint32_t sort_tiles = 0;
@@ -100,6 +101,11 @@ struct msim_ctx {
     double ms[K_COUNT] = {};
     cudaEvent_t t0 = nullptr, t1 = nullptr;
     bool timer_open = false;
+    // the query of tick t runs on qstream while the main stream moves tick t + 1
+    cudaStream_t qstream = nullptr;
+    cudaEvent_t ev_index = nullptr;  // key-start table and sorted positions of tick t ready
+    cudaEvent_t ev_query = nullptr;  // query of tick t done
+    bool query_pending = false;
 
     DeviceMap dmap() const {
         DeviceMap m;
@@ -156,6 +162,9 @@ void free_all(msim_ctx* c) {
     c->pool.clear();
     if (c->t0) cudaEventDestroy(c->t0);
     if (c->t1) cudaEventDestroy(c->t1);
+    if (c->ev_index) cudaEventDestroy(c->ev_index);
+    if (c->ev_query) cudaEventDestroy(c->ev_query);
+    if (c->qstream) cudaStreamDestroy(c->qstream);
     if (c->stream) cudaStreamDestroy(c->stream);
 }
 
@@ -240,6 +249,14 @@ StepLaunch step_args(msim_ctx* c, uint32_t ticks, bool key) {
     return a;
 }
 
+// The main stream waits for a query still running on qstream.
+int join_query(msim_ctx* c) {
+    if (!c->query_pending) return MSIM_OK;
+    CK(cudaStreamWaitEvent(c->stream, c->ev_query, 0), "cudaStreamWaitEvent");
+    c->query_pending = false;
+    return MSIM_OK;
+}
+
 // key + histogram (of the current positions, or after one move tick) + radix sort
 int sort_entities(msim_ctx* c, uint32_t move_ticks) {
     CK(cudaMemsetAsync(c->hist, 0, sizeof(uint32_t) * kMaxPasses * kRadix, c->stream), "memset hist");
@@ -254,6 +271,8 @@ int sort_entities(msim_ctx* c, uint32_t move_ticks) {
     CK(cudaMemsetAsync(c->lookback, 0, sizeof(uint32_t) * (size_t)c->passes * c->sort_tiles * kRadix, c->stream),
        "memset lookback");
     CK(cudaMemsetAsync(c->tickets, 0, sizeof(uint32_t) * kMaxPasses, c->stream), "memset tickets");
+    int rc = join_query(c);  // the passes rewrite the sorted slots the last query reads
+    if (rc != MSIM_OK) return rc;
     for (uint32_t ps = 0; ps < c->passes; ps++) {
         const uint32_t* kin = ps == 0 ? c->key : c->sk[(ps - 1) & 1];
         const uint32_t* vin = ps == 0 ? nullptr : c->sv[(ps - 1) & 1];
@@ -300,16 +319,29 @@ int neighbour_tick(msim_ctx* c) {
         Prof p(c, K_KSTART);
         uint32_t launched = 0;
         CK(launch_kstart(c->stream, c->sorted_key, c->n, c->kstart, (uint32_t)c->num_keys, c->kstart_chunks,
-                         c->kstart_chunk_count, &launched),
+                         c->kstart_chunk_count, &launched, c->sorted_slot, cur_state(c).pos, c->sorted_pos),
            "k_kstart");
         if (launched > 1) c->launch_count += launched - 1;
     }
-    CK(cudaMemsetAsync(c->pairs, 0, sizeof(unsigned long long) * kPairBins, c->stream), "memset pairs");
+    // The query reads only the index (key-start table, sorted slots and positions)
+    // and slot ids: the next tick's move step may overwrite positions meanwhile.  With
+    // profiling on everything stays on one stream so the kernel times do not overlap.
+    cudaStream_t qs = c->stream;
+    if (!c->profiling) {
+        CK(cudaEventRecord(c->ev_index, c->stream), "cudaEventRecord");
+        CK(cudaStreamWaitEvent(c->qstream, c->ev_index, 0), "cudaStreamWaitEvent");
+        qs = c->qstream;
+    }
+    CK(cudaMemsetAsync(c->pairs, 0, sizeof(unsigned long long) * kPairBins, qs), "memset pairs");
     {
         Prof p(c, K_QUERY);
-        CK(launch_query(c->stream, c->params.cap, c->kstart, c->sorted_slot, cur_state(c).pos, cur_state(c).slot_id,
-                        c->grid, c->n, c->nbr_count, c->nbr_list, c->pairs),
+        CK(launch_query(qs, c->params.cap, c->kstart, c->sorted_slot, c->sorted_pos, cur_state(c).slot_id, c->grid,
+                        c->n, c->nbr_count, c->nbr_list, c->pairs),
            "k_query");
+    }
+    if (qs != c->stream) {
+        CK(cudaEventRecord(c->ev_query, qs), "cudaEventRecord");
+        c->query_pending = true;
     }
     c->have_nbr = true;
     c->since_permute++;
@@ -381,8 +413,11 @@ int msim_create(const msim_map* map, const msim_params* params, msim_ctx** out) 
         return code;
     };
     e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->qstream, cudaStreamNonBlocking);
     if (e != cudaSuccess) return bail(cuda_fail(e, "cudaStreamCreate"));
-    if (cudaEventCreate(&c->t0) != cudaSuccess || cudaEventCreate(&c->t1) != cudaSuccess)
+    if (cudaEventCreate(&c->t0) != cudaSuccess || cudaEventCreate(&c->t1) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c->ev_index, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c->ev_query, cudaEventDisableTiming) != cudaSuccess)
         return bail(fail(MSIM_ERR_CUDA, "cudaEventCreate failed"));
 
     // ---- spatial grid ----
@@ -442,6 +477,7 @@ int msim_create(const msim_map* map, const msim_params* params, msim_ctx** out) 
         (rc = dalloc(c, &c->lookback, (size_t)kMaxPasses * c->sort_tiles * kRadix)) ||
         (rc = dalloc(c, &c->tickets, (size_t)kMaxPasses)) || (rc = dalloc(c, &c->kstart, c->num_keys + 1)) ||
         (rc = dalloc(c, &c->kstart_chunks, kstart_chunks(c->num_keys))) || (rc = dalloc(c, &c->kstart_chunk_count, 1)) ||
+        (rc = dalloc(c, &c->sorted_pos, n)) ||
         (rc = dalloc(c, &c->nbr_count, n)) || (rc = dalloc(c, &c->pairs, kPairBins)) || (rc = dalloc(c, &c->err, 1)))
         return bail(rc);
     if (p.cap > 0) {
@@ -550,10 +586,13 @@ int msim_step(msim_ctx* c, uint32_t ticks, uint32_t flags) {
     if (flags & MSIM_STEP_NEIGHBOURS) {
         for (uint32_t t = 0; t < ticks; t++) {
             rc = neighbour_tick(c);
-            if (rc != MSIM_OK) return rc;
+            if (rc != MSIM_OK) {
+                join_query(c);
+                return rc;
+            }
             c->tick++;
         }
-        return MSIM_OK;
+        return join_query(c);  // later work on the context's stream sees the last query
     }
     // move only: up to 256 ticks per launch with the state in registers
     uint32_t left = ticks;

@@ -427,7 +427,8 @@ __device__ __forceinline__ void keep_smallest(uint32_t (&r)[kRegKeep], uint32_t 
 // Exact ascending list of the cap smallest ids of one entity, written by
 // insertion straight into its output slots; for the rare entities with more
 // than kRegKeep neighbours.
-__device__ __noinline__ void list_overflow(const uint32_t* __restrict__ sorted_slot, const float2* __restrict__ pos,
+__device__ __noinline__ void list_overflow(const uint32_t* __restrict__ sorted_slot,
+                                           const float2* __restrict__ sorted_pos,
                                            const uint32_t* __restrict__ slot_id, const uint32_t* __restrict__ kstart,
                                            const TileGrid& g, uint32_t n, uint32_t p, float2 me, uint32_t x0,
                                            uint32_t x1, uint32_t y0, uint32_t y1, uint32_t cap, uint32_t* out) {
@@ -439,8 +440,9 @@ __device__ __noinline__ void list_overflow(const uint32_t* __restrict__ sorted_s
             const uint32_t q1 = kstart[(t + 1u) << g.ybits];
             const uint32_t qend = q1 < n ? q1 : n;
             for (uint32_t q = q0; q < qend; q++) {
+                if (q == p || !in_range(sorted_pos[q], me, g.radius)) continue;
                 const uint32_t s2 = sorted_slot[q];
-                if (q == p || s2 >= n || !in_range(pos[s2], me, g.radius)) continue;
+                if (s2 >= n) continue;
                 const uint32_t oid = slot_id[s2];
                 if (m == cap && oid >= out[cap - 1]) continue;
                 uint32_t j = m < cap ? m++ : cap - 1;
@@ -630,19 +632,25 @@ cudaError_t launch_ranges(cudaStream_t s, const uint32_t* sorted_key, uint32_t n
 uint32_t kstart_chunks(uint64_t num_keys) { return kstart_chunk_cap(num_keys); }
 
 cudaError_t launch_kstart(cudaStream_t s, const uint32_t* sorted_key, uint32_t n, uint32_t* kstart, uint32_t num_keys,
-                          uint4* chunks, uint32_t* chunk_count, uint32_t* kernels) {
+                          uint4* chunks, uint32_t* chunk_count, uint32_t* kernels, const uint32_t* sorted_slot,
+                          const float2* pos, float2* sorted_pos) {
     if (kernels) *kernels = 0;
     if (num_keys == 0) return cudaSuccess;
     if (kernels) *kernels = 1;
     const uint64_t entries = (uint64_t)num_keys + 1u;
+    const bool gather = sorted_slot && pos && sorted_pos && n > 0;
     if ((uint64_t)n > 8u * entries) {  // many positions per key
         k_kstart_search<<<(unsigned)((entries + 255u) / 256u), 256, 0, s>>>(sorted_key, n, kstart, num_keys);
+        if (gather) {
+            k_gather_pos<<<blocks_for(n, 256), 256, 0, s>>>(sorted_slot, pos, n, sorted_pos);
+            if (kernels) *kernels = 2;
+        }
     } else if (chunks && chunk_count) {
         const uint32_t cap = kstart_chunk_cap(num_keys);
         cudaError_t e = cudaMemsetAsync(chunk_count, 0, sizeof(uint32_t), s);
         if (e != cudaSuccess) return e;
         k_kstart_pos<<<blocks_for(n + 1u, 256), 256, 0, s>>>(sorted_key, n, kstart, num_keys, chunks, chunk_count,
-                                                             cap);
+                                                             cap, sorted_slot, pos, sorted_pos);
         e = cudaGetLastError();
         if (e != cudaSuccess) return e;
         int dev = 0, sms = 0;
@@ -653,12 +661,16 @@ cudaError_t launch_kstart(cudaStream_t s, const uint32_t* sorted_key, uint32_t n
     } else {
         const uint64_t warps = (entries + kKstartWindow - 1u) / kKstartWindow;
         k_kstart<<<(unsigned)((warps + 7u) / 8u), 256, 0, s>>>(sorted_key, n, kstart, num_keys);
+        if (gather) {
+            k_gather_pos<<<blocks_for(n, 256), 256, 0, s>>>(sorted_slot, pos, n, sorted_pos);
+            if (kernels) *kernels = 2;
+        }
     }
     return cudaGetLastError();
 }
 
 cudaError_t launch_query(cudaStream_t s, uint32_t cap, const uint32_t* kstart, const uint32_t* sorted_slot,
-                         const float2* pos, const uint32_t* slot_id, TileGrid grid, uint32_t n, uint32_t* count,
+                         const float2* sorted_pos, const uint32_t* slot_id, TileGrid grid, uint32_t n, uint32_t* count,
                          uint32_t* list, unsigned long long* pair_bins) {
     if (n == 0) return cudaSuccess;
     static bool carveout = false;  // 16 blocks of ~9.5 KB per SM
@@ -671,11 +683,11 @@ cudaError_t launch_query(cudaStream_t s, uint32_t cap, const uint32_t* kstart, c
         carveout = true;
     }
     if (cap > 0 && list)
-        k_query<true><<<blocks_for(n, kQueryThreads), kQueryThreads, 0, s>>>(kstart, sorted_slot, pos, slot_id, grid,
-                                                                            n, cap, count, list, pair_bins);
+        k_query<true><<<blocks_for(n, kQueryThreads), kQueryThreads, 0, s>>>(kstart, sorted_slot, sorted_pos, slot_id,
+                                                                            grid, n, cap, count, list, pair_bins);
     else
-        k_query<false><<<blocks_for(n, kQueryThreads), kQueryThreads, 0, s>>>(kstart, sorted_slot, pos, slot_id, grid,
-                                                                             n, 0u, count, nullptr, pair_bins);
+        k_query<false><<<blocks_for(n, kQueryThreads), kQueryThreads, 0, s>>>(kstart, sorted_slot, sorted_pos, slot_id,
+                                                                             grid, n, 0u, count, nullptr, pair_bins);
     return cudaGetLastError();
 }
 

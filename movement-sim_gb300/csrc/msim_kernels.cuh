@@ -56,12 +56,16 @@ cudaError_t launch_ranges(cudaStream_t s, const uint32_t* sorted_key, uint32_t n
                           uint32_t ybits = 0);
 // Key-start table of sorted keys (num_keys + 1 entries).  chunks / chunk_count
 // (kstart_chunks(num_keys) uint4 entries and one counter; may be NULL) enable the
-// per-position kernel.  *kernels (may be NULL) receives the number of kernels launched.
+// per-position kernel, which also gathers pos into sorted order (sorted_pos, n entries)
+// when sorted_slot, pos and sorted_pos are given.  *kernels (may be NULL) receives the
+// number of kernels launched.
 uint32_t kstart_chunks(uint64_t num_keys);
 cudaError_t launch_kstart(cudaStream_t s, const uint32_t* sorted_key, uint32_t n, uint32_t* kstart, uint32_t num_keys,
-                          uint4* chunks = nullptr, uint32_t* chunk_count = nullptr, uint32_t* kernels = nullptr);
+                          uint4* chunks = nullptr, uint32_t* chunk_count = nullptr, uint32_t* kernels = nullptr,
+                          const uint32_t* sorted_slot = nullptr, const float2* pos = nullptr,
+                          float2* sorted_pos = nullptr);
 cudaError_t launch_query(cudaStream_t s, uint32_t cap, const uint32_t* kstart, const uint32_t* sorted_slot,
-                         const float2* pos, const uint32_t* slot_id, TileGrid grid, uint32_t n, uint32_t* count,
+                         const float2* sorted_pos, const uint32_t* slot_id, TileGrid grid, uint32_t n, uint32_t* count,
                          uint32_t* list, unsigned long long* pair_bins);  // pair_bins: kPairBins counters
 cudaError_t launch_iota(cudaStream_t s, uint32_t* out, uint32_t n);
 cudaError_t launch_permute(cudaStream_t s, const uint32_t* sorted_slot, EntityState src,

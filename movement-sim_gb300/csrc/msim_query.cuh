@@ -95,10 +95,15 @@ constexpr uint32_t kGapChunk = 4096;
 __global__ __launch_bounds__(256) void k_kstart_pos(const uint32_t* __restrict__ sk, uint32_t n,
                                                     uint32_t* __restrict__ kstart, uint32_t num_keys,
                                                     uint4* __restrict__ chunks, uint32_t* chunk_count,
-                                                    uint32_t chunk_cap) {
+                                                    uint32_t chunk_cap, const uint32_t* __restrict__ sv,
+                                                    const float2* __restrict__ pos, float2* __restrict__ sorted_pos) {
     constexpr uint32_t FULL = 0xffffffffu;
     const uint32_t lane = threadIdx.x & 31;
     const uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (sorted_pos && q < n) {  // positions in sorted order, for the query's candidate reads
+        const uint32_t slot = sv[q];
+        sorted_pos[q] = slot < n ? pos[slot] : make_float2(__int_as_float(0x7fffffff), __int_as_float(0x7fffffff));
+    }
     uint32_t from = 0, len = 0;
     if (q <= n) {
         from = q ? clamped_key(sk, q - 1u, num_keys) + 1u : 0u;
@@ -177,6 +182,16 @@ inline uint32_t kstart_chunk_cap(uint64_t num_keys) {
     return (uint32_t)((num_keys + 1u) / (kGapWarp + 1u) + (num_keys + 1u) / kGapChunk + 2u);
 }
 
+// Positions in sorted order (NaN for a slot out of range), for the key-start paths
+// that do not gather them on the way.
+__global__ __launch_bounds__(256) void k_gather_pos(const uint32_t* __restrict__ sv, const float2* __restrict__ pos,
+                                                    uint32_t n, float2* __restrict__ sorted_pos) {
+    const uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= n) return;
+    const uint32_t slot = sv[q];
+    sorted_pos[q] = slot < n ? pos[slot] : make_float2(__int_as_float(0x7fffffff), __int_as_float(0x7fffffff));
+}
+
 // One thread per table entry, binary search over the sorted keys: for key spaces
 // much smaller than the number of positions (many positions per key).
 __global__ __launch_bounds__(256) void k_kstart_search(const uint32_t* __restrict__ sk, uint32_t n,
@@ -205,8 +220,9 @@ __global__ __launch_bounds__(256) void k_kstart_search(const uint32_t* __restric
 // tests 32 (owner, candidate) pairs per iteration, so every lane is busy whatever the
 // run lengths; the run of each pair comes from a bit mask of the runs that start in
 // the current window of 32 pairs.  Every candidate is tested with the predicate of
-// random_move.comp:551-562.  A hit adds one to the owner's count and, for the first
-// kRegKeep hits, keeps the candidate's slot; ids are looked up only for those.  An
+// random_move.comp:551-562; candidate positions come from the sorted copy, read in
+// runs.  A hit adds one to the owner's count and, for the first kRegKeep hits,
+// keeps the candidate's sorted position; ids are looked up only for those.  An
 // entity with more than kRegKeep neighbours redoes an exact pass into its output
 // slots.  The predicate is symmetric (fl(a - b) = -fl(b - a)), so the pair count is
 // half the sum of the counts.  Each warp writes its lists contiguously at
@@ -218,7 +234,7 @@ constexpr uint32_t kWarpRuns = 32u * kRuns;    // run-list capacity of a warp
 struct QueryShared {
     float2 me[kQueryThreads];
     uint32_t cnt[kQueryThreads];
-    uint32_t keep[kRegKeep][kQueryThreads];    // slots of the first kRegKeep hits
+    uint32_t keep[kRegKeep][kQueryThreads];    // sorted positions of the first kRegKeep hits
     uint32_t rq[kQueryThreads / 32][kWarpRuns];   // run start position minus its flat start
     uint32_t rfs[kQueryThreads / 32][kWarpRuns];  // flat start of the run
     uint32_t rown[kQueryThreads / 32][kWarpRuns]; // owner lane
@@ -227,8 +243,7 @@ struct QueryShared {
 template <bool LIST>
 __device__ __forceinline__ void query_runs(const uint32_t (&lo)[kRuns], const uint32_t (&len)[kRuns], uint32_t lane,
                                            uint32_t warp, uint32_t pwarp, QueryShared& sh,
-                                           const uint32_t* __restrict__ sorted_slot, const float2* __restrict__ pos,
-                                           const TileGrid& g, uint32_t n) {
+                                           const float2* __restrict__ sorted_pos, const TileGrid& g) {
     constexpr uint32_t FULL = 0xffffffffu;
     uint32_t flat = 0, nr = 0;
 #pragma unroll
@@ -273,12 +288,10 @@ __device__ __forceinline__ void query_runs(const uint32_t (&lo)[kRuns], const ui
         const uint32_t q = sh.rq[warp][run] + i;
         const uint32_t owner = sh.rown[warp][run];
         if (q == pwarp + owner) continue;  // the owner itself
-        const uint32_t s2 = sorted_slot[q];
-        if (s2 >= n) continue;
         const uint32_t ot = warp * 32u + owner;
-        if (!in_range_fast(pos[s2], sh.me[ot], g.radius, g.d2_limit)) continue;
+        if (!in_range_fast(sorted_pos[q], sh.me[ot], g.radius, g.d2_limit)) continue;
         const uint32_t c = atomicAdd(&sh.cnt[ot], 1u);
-        if (LIST && c < (uint32_t)kRegKeep) sh.keep[c][ot] = s2;
+        if (LIST && c < (uint32_t)kRegKeep) sh.keep[c][ot] = q;  // sorted position; the id comes later
     }
     __syncwarp();  // before the run list is rewritten
 }
@@ -286,7 +299,7 @@ __device__ __forceinline__ void query_runs(const uint32_t (&lo)[kRuns], const ui
 template <bool LIST>
 __global__ __launch_bounds__(kQueryThreads) void k_query(const uint32_t* __restrict__ kstart,
                                                          const uint32_t* __restrict__ sorted_slot,
-                                                         const float2* __restrict__ pos,
+                                                         const float2* __restrict__ sorted_pos,
                                                          const uint32_t* __restrict__ slot_id, TileGrid g,
                                                          uint32_t n, uint32_t cap, uint32_t* __restrict__ count_out,
                                                          uint32_t* __restrict__ list,
@@ -303,8 +316,7 @@ __global__ __launch_bounds__(kQueryThreads) void k_query(const uint32_t* __restr
     uint32_t x0 = 1, x1 = 0, y0 = 1, y1 = 0;  // empty box for invalid lanes
     float ylo = 0.f, yhi = 0.f;
     if (valid) {
-        const uint32_t s = sorted_slot[p] < n ? sorted_slot[p] : 0u;
-        me = pos[s];
+        me = sorted_pos[p];
         ylo = __fsub_rn(me.y, g.reach);
         yhi = __fadd_rn(me.y, g.reach);
         x0 = tile_coord(__fsub_rn(me.x, g.reach), g.inv_cell, g.tiles_x);
@@ -342,7 +354,7 @@ __global__ __launch_bounds__(kQueryThreads) void k_query(const uint32_t* __restr
                 len[k] = hi > lo[k] ? hi - lo[k] : 0u;
             }
         }
-        query_runs<LIST>(lo, len, lane, warp, pwarp, sh, sorted_slot, pos, g, n);
+        query_runs<LIST>(lo, len, lane, warp, pwarp, sh, sorted_pos, g);
     } else {
         // general boxes (tile side below 2 x reach): kRuns tiles per round
         const uint32_t nslots = nx * ny;
@@ -367,7 +379,7 @@ __global__ __launch_bounds__(kQueryThreads) void k_query(const uint32_t* __restr
                     len[k] = hi > lo[k] ? hi - lo[k] : 0u;
                 }
             }
-            query_runs<LIST>(lo, len, lane, warp, pwarp, sh, sorted_slot, pos, g, n);
+            query_runs<LIST>(lo, len, lane, warp, pwarp, sh, sorted_pos, g);
         }
     }
     __syncwarp();
@@ -387,7 +399,10 @@ __global__ __launch_bounds__(kQueryThreads) void k_query(const uint32_t* __restr
         if (count <= (uint32_t)kRegKeep) {  // every neighbour is kept: ids, sort, write
             uint32_t keep[kRegKeep];
 #pragma unroll
-            for (int i = 0; i < kRegKeep; i++) keep[i] = (uint32_t)i < count ? slot_id[sh.keep[i][tid]] : 0xffffffffu;
+            for (int i = 0; i < kRegKeep; i++) {
+                const uint32_t s2 = (uint32_t)i < count ? sorted_slot[sh.keep[i][tid]] : n;
+                keep[i] = s2 < n ? slot_id[s2] : 0xffffffffu;
+            }
 #pragma unroll
             for (int a = 0; a < kRegKeep; a++)
 #pragma unroll
@@ -401,7 +416,7 @@ __global__ __launch_bounds__(kQueryThreads) void k_query(const uint32_t* __restr
             for (int i = 0; i < kRegKeep; i++)
                 if ((uint32_t)i < kept) out[i] = keep[i];
         } else {
-            list_overflow(sorted_slot, pos, slot_id, kstart, g, n, p, me, x0, x1, y0, y1, cap, out);
+            list_overflow(sorted_slot, sorted_pos, slot_id, kstart, g, n, p, me, x0, x1, y0, y1, cap, out);
         }
     }
 }

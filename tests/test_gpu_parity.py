@@ -215,6 +215,25 @@ def test_crowd_beyond_cap_and_radius_boundary(msim, orc):
     assert cnt[210] == 49  # not the entities at distance exactly R
 
 
+def test_coarse_tiles_many_entities_per_key(msim, orc):
+    """200 m tiles on a 380 m lattice: 2 x 2 tiles and 64 bands give 256 keys for 3000
+    entities, so the key-start table comes from the per-key search kernel."""
+    road_map = msim.RoadMap.lattice(8, 2)
+    n = 3000
+    with msim.Simulation(road_map, n, rng="pcg32", dt=0.1, radius=2.0, cap=16, cell_size=200.0) as sim:
+        assert (1 << sim.info()["key_bits"]) * 8 < n
+        sim.init_entities(9, placement="fraction", speed=(1.0, 1.6))
+        pos, head, rng, speed = _oracle_state(orc, road_map, n, 1, 9, 1, (1.0, 1.6))
+        for _ in range(3):
+            sim.step(2, neighbours=True)
+            orc.step(road_map.road_pos, road_map.road_conn, road_map.connections, pos, head, rng, speed, 1, 0.1, 2)
+            _assert_state(sim.get_state(), pos, head, rng)
+            cnt, idx = sim.get_neighbours()
+            ocnt, oidx, opairs = orc.neighbours(pos, 2.0, 16)
+            assert np.array_equal(cnt, ocnt) and np.array_equal(idx, oidx)
+            assert sim.collision_pairs() == opairs
+
+
 @pytest.mark.parametrize("radius", [2.0, 0.3, 1.7, 5.55])
 def test_radius_predicate_ulp_boundary(msim, orc, radius):
     """Pairs whose distance lies within a few ulps of R at random angles: the
