@@ -522,7 +522,8 @@ def cpu_baseline(cfg, road_map, budget_s=20.0, kind="port"):
         if el > budget_s or ticks >= (sample["ticks"]):
             break
     return {"value": n * ticks / el, "unit": "entity-steps/s", "cores": threads, "kind": kind,
-            "sample": f"{ticks} ticks of {desc}: oracle C restatement (move + CPU-grid neighbour query), "
+            "sample": f"{ticks} ticks of {desc}: oracle C restatement ("
+                      f"{'move + CPU-grid neighbour query' if sample['neighbours'] else 'move only'}), "
                       f"{threads} threads"}
 
 

@@ -78,6 +78,7 @@ struct msim_ctx {
     unsigned long long* pairs = nullptr;
     bool have_nbr = false;
     uint32_t* err = nullptr;
+    uint32_t* check = nullptr;  // first invalid heading found by msim_set_entities
     TileGrid grid{};
     uint32_t passes = 1;
     uint32_t resort = 16;
@@ -478,7 +479,8 @@ int msim_create(const msim_map* map, const msim_params* params, msim_ctx** out) 
         (rc = dalloc(c, &c->tickets, (size_t)kMaxPasses)) || (rc = dalloc(c, &c->kstart, c->num_keys + 1)) ||
         (rc = dalloc(c, &c->kstart_chunks, kstart_chunks(c->num_keys))) || (rc = dalloc(c, &c->kstart_chunk_count, 1)) ||
         (rc = dalloc(c, &c->sorted_pos, n)) ||
-        (rc = dalloc(c, &c->nbr_count, n)) || (rc = dalloc(c, &c->pairs, kPairBins)) || (rc = dalloc(c, &c->err, 1)))
+        (rc = dalloc(c, &c->nbr_count, n)) || (rc = dalloc(c, &c->pairs, kPairBins)) || (rc = dalloc(c, &c->err, 1)) ||
+        (rc = dalloc(c, &c->check, 1)))
         return bail(rc);
     if (p.cap > 0) {
         size_t blocks = (n + kQueryThreads - 1) / kQueryThreads;
@@ -539,25 +541,28 @@ int msim_set_entities(msim_ctx* c, const float* pos, const uint32_t* heading, co
     int rc = check_ctx(c);
     if (rc != MSIM_OK) return rc;
     if (c->n && (!pos || !heading || !rng)) return fail(MSIM_ERR_INVALID, "pos, heading and rng are required");
-    for (uint32_t i = 0; i < c->n; i++)
-        if ((heading[i] & MSIM_HEADING_ROAD_MASK) >= c->R)
-            return fail(MSIM_ERR_OOB, "heading of entity " + std::to_string(i) + " names road " +
-                                          std::to_string(heading[i] & MSIM_HEADING_ROAD_MASK) + " of " +
-                                          std::to_string(c->R));
-    c->cur = 0;
-    EntityState& s = c->st[0];
     const size_t n = c->n;
     if (n == 0) return MSIM_OK;
-    CK(cudaMemcpyAsync(s.pos, pos, sizeof(float2) * n, cudaMemcpyHostToDevice, c->stream), "upload pos");
+    // upload into the spare state buffer; it becomes current once the headings are checked
+    const int b = 1 - c->cur;
+    EntityState& s = c->st[b];
     CK(cudaMemcpyAsync(s.head, heading, sizeof(uint32_t) * n, cudaMemcpyHostToDevice, c->stream), "upload heading");
+    CK(launch_check_roads(c->stream, s.head, c->n, c->R, c->check), "k_check_roads");
+    CK(cudaMemcpyAsync(s.pos, pos, sizeof(float2) * n, cudaMemcpyHostToDevice, c->stream), "upload pos");
     CK(cudaMemcpyAsync(s.rng, rng, sizeof(uint4) * n, cudaMemcpyHostToDevice, c->stream), "upload rng");
     if (speed) {
         CK(cudaMemcpyAsync(s.speed, speed, sizeof(float) * n, cudaMemcpyHostToDevice, c->stream), "upload speed");
     } else {
-        std::vector<float> sp(n, 1.4f);
-        CK(cudaMemcpyAsync(s.speed, sp.data(), sizeof(float) * n, cudaMemcpyHostToDevice, c->stream), "upload speed");
-        CK(cudaStreamSynchronize(c->stream), "sync");
+        CK(launch_fill(c->stream, s.speed, c->n, 1.4f), "k_fill");  // SPEED, random_move.comp:750
     }
+    uint32_t first_bad = 0;
+    CK(cudaMemcpyAsync(&first_bad, c->check, sizeof(first_bad), cudaMemcpyDeviceToHost, c->stream), "read check");
+    CK(cudaStreamSynchronize(c->stream), "cudaStreamSynchronize");
+    if (first_bad != 0xffffffffu)
+        return fail(MSIM_ERR_OOB, "heading of entity " + std::to_string(first_bad) + " names road " +
+                                      std::to_string(heading[first_bad] & MSIM_HEADING_ROAD_MASK) + " of " +
+                                      std::to_string(c->R));
+    c->cur = b;
     // entity i starts in slot i
     CK(launch_iota(c->stream, s.slot_id, c->n), "k_iota");
     return build_index(c);

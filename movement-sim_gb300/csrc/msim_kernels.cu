@@ -554,6 +554,19 @@ __global__ void k_export_colors(const uint32_t* sorted_slot, const uint32_t* slo
                                      __float_as_uint(1.f));
 }
 
+// First entity whose heading names a road >= num_roads (atomicMin into *first_bad).
+__global__ void k_check_roads(const uint32_t* __restrict__ head, uint32_t n, uint32_t num_roads, uint32_t* first_bad) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool bad = i < n && (head[i] & kHeadRoad) >= num_roads;
+    const unsigned m = __ballot_sync(0xffffffffu, bad);
+    if (m && (threadIdx.x & 31) == (uint32_t)(__ffs(m) - 1)) atomicMin(first_bad, i);
+}
+
+__global__ void k_fill_f32(float* out, uint32_t n, float v) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] = v;
+}
+
 __global__ void k_iota(uint32_t* out, uint32_t n) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) out[i] = i;
@@ -688,6 +701,20 @@ cudaError_t launch_query(cudaStream_t s, uint32_t cap, const uint32_t* kstart, c
     else
         k_query<false><<<blocks_for(n, kQueryThreads), kQueryThreads, 0, s>>>(kstart, sorted_slot, sorted_pos, slot_id,
                                                                              grid, n, 0u, count, nullptr, pair_bins);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_check_roads(cudaStream_t s, const uint32_t* head, uint32_t n, uint32_t num_roads,
+                               uint32_t* first_bad) {
+    cudaError_t e = cudaMemsetAsync(first_bad, 0xff, sizeof(uint32_t), s);
+    if (e != cudaSuccess || n == 0) return e;
+    k_check_roads<<<blocks_for(n, 256), 256, 0, s>>>(head, n, num_roads, first_bad);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_fill(cudaStream_t s, float* out, uint32_t n, float v) {
+    if (n == 0) return cudaSuccess;
+    k_fill_f32<<<blocks_for(n, 256), 256, 0, s>>>(out, n, v);
     return cudaGetLastError();
 }
 

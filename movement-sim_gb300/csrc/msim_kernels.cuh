@@ -68,6 +68,10 @@ cudaError_t launch_query(cudaStream_t s, uint32_t cap, const uint32_t* kstart, c
                          const float2* sorted_pos, const uint32_t* slot_id, TileGrid grid, uint32_t n, uint32_t* count,
                          uint32_t* list, unsigned long long* pair_bins);  // pair_bins: kPairBins counters
 cudaError_t launch_iota(cudaStream_t s, uint32_t* out, uint32_t n);
+// *first_bad = first i with (head[i] & road mask) >= num_roads, or 0xffffffff
+cudaError_t launch_check_roads(cudaStream_t s, const uint32_t* head, uint32_t n, uint32_t num_roads,
+                               uint32_t* first_bad);
+cudaError_t launch_fill(cudaStream_t s, float* out, uint32_t n, float v);
 cudaError_t launch_permute(cudaStream_t s, const uint32_t* sorted_slot, EntityState src,
                            EntityState dst, uint32_t n);
 cudaError_t launch_export_state(cudaStream_t s, EntityState st, uint32_t n, float2* pos,
