@@ -123,8 +123,13 @@ typedef struct msim_params {
     uint32_t cap;             /* neighbours kept per entity, ascending id (0 = count only) */
     float cell_size;          /* spatial tile side in metres; 0 = automatic */
     uint32_t resort_interval; /* ticks between re-orderings of the entity state; 0 = automatic */
-    uint32_t flags;           /* reserved, must be 0 */
+    uint32_t flags;           /* MSIM_PARAM_* bits */
 } msim_params;
+
+/* msim_params.flags: rebuild the index by a full radix sort every neighbour tick
+ * instead of updating the previous order (same results; for entities that move far
+ * between ticks, where most keys change). */
+#define MSIM_PARAM_FULL_SORT 1u
 
 typedef struct msim_init {
     uint64_t seed;

@@ -26,6 +26,7 @@ HEADING_ROAD_MASK = 0x7FFFFFFF
 PLACE_ROAD_START = 0
 PLACE_UNIFORM_FRACTION = 1
 STEP_NEIGHBOURS = 1
+PARAM_FULL_SORT = 1
 NO_NEIGHBOUR = 0xFFFFFFFF
 
 

@@ -32,10 +32,13 @@ enum KernelId : uint32_t {
     K_QUERY,
     K_PERMUTE,
     K_EXPORT,
+    K_MARK,   // split of the previous order into unchanged / changed keys
+    K_MERGE,  // merge + key-start table + sorted positions
     K_COUNT
 };
-static const char* const kKernelNames[K_COUNT] = {"k_init",   "k_step",  "k_step_multi", "k_hist_scan", "k_onesweep",
-                                                  "k_kstart", "k_query", "k_permute",    "k_export"};
+static const char* const kKernelNames[K_COUNT] = {"k_init",   "k_step",    "k_step_multi", "k_hist_scan",
+                                                  "k_onesweep", "k_kstart", "k_query",     "k_permute",
+                                                  "k_export", "k_mark",    "k_merge"};
 
 }  // namespace msim
 
@@ -72,6 +75,18 @@ struct msim_ctx {
     const uint32_t* sorted_key = nullptr;
     const uint32_t* sorted_slot = nullptr;
     bool have_sort = false;
+    // incremental index update: the previous order split into unchanged (a) and
+    // changed (b, sorted in place with ping-pong) keys, then merged
+    bool order_identity = false;  // sorted_slot[q] == q (right after a re-ordering)
+    bool incremental = true;      // index updates from the previous order (else full sorts)
+    uint32_t* a_key = nullptr;
+    uint32_t* a_val = nullptr;
+    uint32_t* b_key[2] = {nullptr, nullptr};
+    uint32_t* b_val[2] = {nullptr, nullptr};
+    uint32_t* ab_counts = nullptr;
+    unsigned long long* mark_lookback = nullptr;
+    uint32_t* mark_ticket = nullptr;
+    uint32_t* merge_split = nullptr;
     // neighbours
     uint32_t* nbr_count = nullptr;
     uint32_t* nbr_list = nullptr;
@@ -294,6 +309,7 @@ int permute_state(msim_ctx* c) {
     CK(launch_permute(c->stream, c->sorted_slot, c->st[c->cur], c->st[1 - c->cur], c->n), "k_permute");
     c->cur = 1 - c->cur;
     c->have_sort = false;
+    c->order_identity = true;  // slot q now holds the entity at sorted position q
     c->since_permute = 0;
     return MSIM_OK;
 }
@@ -308,15 +324,72 @@ int build_index(msim_ctx* c) {
     return permute_state(c);
 }
 
+// One tick of the move plus the index, from the previous sorted order: split it by
+// whether each key changed, sort the changed entries, merge (writing the key-start
+// table and the sorted positions on the way).
+int incremental_index(msim_ctx* c) {
+    CK(cudaMemsetAsync(c->hist, 0, sizeof(uint32_t) * kMaxPasses * kRadix, c->stream), "memset hist");
+    {
+        Prof p(c, K_STEP);
+        StepLaunch a = step_args(c, 1, true);
+        a.hist = nullptr;  // the changed keys' digits are counted by k_mark
+        CK(launch_step(c->stream, a), "k_step");
+    }
+    {
+        Prof p(c, K_MARK);
+        CK(launch_mark(c->stream, c->sorted_slot, c->order_identity, c->sorted_key, c->key, c->n, c->passes,
+                       c->a_key, c->a_val, c->b_key[0], c->b_val[0], c->hist, c->mark_lookback, c->mark_ticket,
+                       c->ab_counts, c->err),
+           "k_mark");
+    }
+    {
+        Prof p(c, K_HIST_SCAN);
+        CK(launch_hist_scan(c->stream, c->hist, c->digit_off, c->passes), "k_hist_scan");
+    }
+    CK(cudaMemsetAsync(c->lookback, 0, sizeof(uint32_t) * (size_t)c->passes * c->sort_tiles * kRadix, c->stream),
+       "memset lookback");
+    CK(cudaMemsetAsync(c->tickets, 0, sizeof(uint32_t) * kMaxPasses, c->stream), "memset tickets");
+    for (uint32_t ps = 0; ps < c->passes; ps++) {  // stable radix sort of the changed entries
+        Prof p(c, K_SORT_PASS);
+        CK(launch_onesweep(c->stream, c->b_key[ps & 1], c->b_val[ps & 1], c->b_key[(ps + 1) & 1],
+                           c->b_val[(ps + 1) & 1], c->n, 8u * ps, c->digit_off + ps * kRadix,
+                           c->lookback + (size_t)ps * c->sort_tiles * kRadix, c->tickets + ps, c->err,
+                           c->ab_counts + 1),
+           "k_onesweep");
+    }
+    int rc = join_query(c);  // the merge rewrites the table and sorted positions the last query reads
+    if (rc != MSIM_OK) return rc;
+    const int out = c->sorted_key == c->sk[0] ? 1 : 0;
+    {
+        Prof p(c, K_MERGE);
+        uint32_t launched = 0;
+        CK(launch_merge(c->stream, c->a_key, c->a_val, c->b_key[c->passes & 1], c->b_val[c->passes & 1],
+                        c->ab_counts, c->merge_split, c->n, c->sk[out], c->sv[out], cur_state(c).pos, c->sorted_pos,
+                        c->kstart, (uint32_t)c->num_keys, c->kstart_chunks, c->kstart_chunk_count, c->err,
+                        &launched),
+           "k_merge");
+        if (launched > 1) c->launch_count += launched - 1;
+    }
+    c->sorted_key = c->sk[out];
+    c->sorted_slot = c->sv[out];
+    c->order_identity = false;
+    c->have_sort = true;
+    return MSIM_OK;
+}
+
 int neighbour_tick(msim_ctx* c) {
     int rc;
     if (c->have_sort && c->since_permute >= c->resort) {
         rc = permute_state(c);
         if (rc != MSIM_OK) return rc;
     }
-    rc = sort_entities(c, 1);
-    if (rc != MSIM_OK) return rc;
-    {
+    if (c->sorted_key && c->incremental) {
+        rc = incremental_index(c);
+        if (rc != MSIM_OK) return rc;
+    } else {
+        rc = sort_entities(c, 1);
+        if (rc != MSIM_OK) return rc;
+        c->order_identity = false;
         Prof p(c, K_KSTART);
         uint32_t launched = 0;
         CK(launch_kstart(c->stream, c->sorted_key, c->n, c->kstart, (uint32_t)c->num_keys, c->kstart_chunks,
@@ -392,7 +465,7 @@ int msim_create(const msim_map* map, const msim_params* params, msim_ctx** out) 
     if (!std::isfinite(p.radius) || p.radius < 0.f) return fail(MSIM_ERR_INVALID, "radius must be finite and >= 0");
     if (p.cap > kMaxCap) return fail(MSIM_ERR_INVALID, "cap must be <= " + std::to_string(kMaxCap));
     if (p.cell_size < 0.f || !std::isfinite(p.cell_size)) return fail(MSIM_ERR_INVALID, "cell_size must be >= 0");
-    if (p.flags != 0) return fail(MSIM_ERR_INVALID, "flags must be 0");
+    if (p.flags & ~MSIM_PARAM_FULL_SORT) return fail(MSIM_ERR_INVALID, "unknown params flags");
 
     msim_ctx* c = new (std::nothrow) msim_ctx();
     if (!c) return fail(MSIM_ERR_NOMEM, "out of host memory");
@@ -402,6 +475,7 @@ int msim_create(const msim_map* map, const msim_params* params, msim_ctx** out) 
         return cuda_fail(e, "cudaGetDevice");
     }
     c->params = p;
+    c->incremental = (p.flags & MSIM_PARAM_FULL_SORT) == 0;
     c->n = p.num_entities;
     c->R = map->num_roads;
     c->C = map->num_connections;
@@ -478,7 +552,11 @@ int msim_create(const msim_map* map, const msim_params* params, msim_ctx** out) 
         (rc = dalloc(c, &c->lookback, (size_t)kMaxPasses * c->sort_tiles * kRadix)) ||
         (rc = dalloc(c, &c->tickets, (size_t)kMaxPasses)) || (rc = dalloc(c, &c->kstart, c->num_keys + 1)) ||
         (rc = dalloc(c, &c->kstart_chunks, kstart_chunks(c->num_keys))) || (rc = dalloc(c, &c->kstart_chunk_count, 1)) ||
-        (rc = dalloc(c, &c->sorted_pos, n)) ||
+        (rc = dalloc(c, &c->sorted_pos, n)) || (rc = dalloc(c, &c->a_key, n)) || (rc = dalloc(c, &c->a_val, n)) ||
+        (rc = dalloc(c, &c->b_key[0], n)) || (rc = dalloc(c, &c->b_key[1], n)) || (rc = dalloc(c, &c->b_val[0], n)) ||
+        (rc = dalloc(c, &c->b_val[1], n)) || (rc = dalloc(c, &c->ab_counts, 2)) ||
+        (rc = dalloc(c, &c->mark_lookback, mark_tiles(c->n))) || (rc = dalloc(c, &c->mark_ticket, 1)) ||
+        (rc = dalloc(c, &c->merge_split, (size_t)merge_tiles(c->n) + 1)) ||
         (rc = dalloc(c, &c->nbr_count, n)) || (rc = dalloc(c, &c->pairs, kPairBins)) || (rc = dalloc(c, &c->err, 1)) ||
         (rc = dalloc(c, &c->check, 1)))
         return bail(rc);

@@ -188,12 +188,12 @@ __global__ __launch_bounds__(kStepThreads) void k_step(StepLaunch a) {
                 a.key[sl[u]] = key[u];
             }
         }
-        if (KEY) {
+        if (KEY && a.hist) {
             digit_counts<RNG, KEY>(key[0], valid[0], lane, a.passes, s_hist);
             digit_counts<RNG, KEY>(key[1], valid[1], lane, a.passes, s_hist);
         }
     }
-    if (KEY) {
+    if (KEY && a.hist) {
         __syncthreads();
         for (uint32_t i = threadIdx.x; i < a.passes * kRadix; i += kStepThreads) {
             const uint32_t c = s_hist[i];
@@ -224,13 +224,15 @@ __global__ __launch_bounds__(kRadix) void k_hist_scan(const uint32_t* hist, uint
 // stable; (3) the previous counts are broadcast from the leaders (steps 2 and 3
 // four rows at a time).  Values are read
 // only for the local scatter, so they hold no registers during the ranking.
+template <bool PERSIST>
 __global__ __launch_bounds__(kSortThreads, 4) void k_onesweep(const uint32_t* __restrict__ keys_in,
                                                               const uint32_t* __restrict__ vals_in,
                                                               uint32_t* __restrict__ keys_out,
                                                               uint32_t* __restrict__ vals_out, uint32_t n,
                                                               uint32_t shift,
                                                               const uint32_t* __restrict__ digit_offset,
-                                                              uint32_t* lookback, uint32_t* ticket, uint32_t* err) {
+                                                              uint32_t* lookback, uint32_t* ticket, uint32_t* err,
+                                                              const uint32_t* __restrict__ n_dev) {
     constexpr int NW = kSortThreads / 32;
     constexpr uint32_t FULL = 0xffffffffu;
     __shared__ uint32_t s_keys[kSortTile];
@@ -242,10 +244,15 @@ __global__ __launch_bounds__(kSortThreads, 4) void k_onesweep(const uint32_t* __
     __shared__ uint32_t s_tile;
 
     const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    if (n_dev) n = min(*n_dev, n);  // item count known only on the device (grid sized for n)
+    const uint32_t tiles = n ? (n + kSortTile - 1u) / kSortTile : 1u;
+  for (;;) {  // a block takes tiles until none is left (the grid may be smaller than the tiles)
+    __syncthreads();  // the previous tile's shared memory is free
     if (tid == 0) s_tile = atomicAdd(ticket, 1u);
     for (uint32_t i = tid; i < NW * kRadix; i += kSortThreads) s_whist[i] = 0u;
     __syncthreads();
     const uint32_t tile = s_tile;
+    if (tile >= tiles) return;  // tiles past the end: no later tile waits for them
     const uint32_t base = tile * kSortTile;
     const uint32_t row0 = base + warp * (kSortRows * 32) + lane;
 
@@ -377,6 +384,8 @@ __global__ __launch_bounds__(kSortThreads, 4) void k_onesweep(const uint32_t* __
         keys_out[g] = key;
         vals_out[g] = s_vals[i];
     }
+    if (!PERSIST) return;  // one tile per block
+  }
 }
 
 // [start, end) of every occupied tile; the tile of a key is key >> ybits.
@@ -457,6 +466,7 @@ __device__ __noinline__ void list_overflow(const uint32_t* __restrict__ sorted_s
 }
 
 #include "msim_query.cuh"
+#include "msim_incsort.cuh"
 
 __global__ void k_permute(const uint32_t* __restrict__ ss, EntityState src, EntityState dst, uint32_t n) {
     const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
@@ -621,16 +631,29 @@ cudaError_t launch_hist_scan(cudaStream_t s, const uint32_t* hist, uint32_t* off
 
 cudaError_t launch_onesweep(cudaStream_t s, const uint32_t* keys_in, const uint32_t* vals_in, uint32_t* keys_out,
                             uint32_t* vals_out, uint32_t n, uint32_t shift, const uint32_t* digit_offset,
-                            uint32_t* lookback, uint32_t* ticket, uint32_t* err) {
+                            uint32_t* lookback, uint32_t* ticket, uint32_t* err, const uint32_t* n_dev) {
     if (n == 0) return cudaSuccess;
     static bool carveout = false;  // prefer the largest shared-memory carveout: 4 blocks of 43 KB per SM
     if (!carveout) {
-        cudaFuncSetAttribute(k_onesweep, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
+        cudaFuncSetAttribute(k_onesweep<false>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                             cudaSharedmemCarveoutMaxShared);
+        cudaFuncSetAttribute(k_onesweep<true>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                             cudaSharedmemCarveoutMaxShared);
         cudaGetLastError();
         carveout = true;
     }
-    k_onesweep<<<blocks_for(n, kSortTile), kSortThreads, 0, s>>>(keys_in, vals_in, keys_out, vals_out, n, shift,
-                                                                 digit_offset, lookback, ticket, err);
+    unsigned grid = blocks_for(n, kSortTile);
+    if (n_dev) {  // count known on the device only: a resident grid that loops over tiles
+        int dev = 0, sms = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        grid = std::min<unsigned>(grid, 4u * (unsigned)(sms > 0 ? sms : 1));
+        k_onesweep<true><<<grid, kSortThreads, 0, s>>>(keys_in, vals_in, keys_out, vals_out, n, shift, digit_offset,
+                                                       lookback, ticket, err, n_dev);
+        return cudaGetLastError();
+    }
+    k_onesweep<false><<<grid, kSortThreads, 0, s>>>(keys_in, vals_in, keys_out, vals_out, n, shift,
+                                                                 digit_offset, lookback, ticket, err, n_dev);
     return cudaGetLastError();
 }
 
@@ -715,6 +738,48 @@ cudaError_t launch_check_roads(cudaStream_t s, const uint32_t* head, uint32_t n,
 cudaError_t launch_fill(cudaStream_t s, float* out, uint32_t n, float v) {
     if (n == 0) return cudaSuccess;
     k_fill_f32<<<blocks_for(n, 256), 256, 0, s>>>(out, n, v);
+    return cudaGetLastError();
+}
+
+uint32_t mark_tiles(uint32_t n) { return (n + kMarkTile - 1u) / kMarkTile; }
+uint32_t merge_tiles(uint32_t n) { return (n + kMergeTile - 1u) / kMergeTile; }
+
+cudaError_t launch_mark(cudaStream_t s, const uint32_t* P, bool identity, const uint32_t* PK, const uint32_t* NK,
+                        uint32_t n, uint32_t passes, uint32_t* a_key, uint32_t* a_val, uint32_t* b_key,
+                        uint32_t* b_val, uint32_t* hist, unsigned long long* lookback, uint32_t* ticket,
+                        uint32_t* counts, uint32_t* err) {
+    if (n == 0) return cudaMemsetAsync(counts, 0, 2 * sizeof(uint32_t), s);
+    const uint32_t tiles = mark_tiles(n);
+    cudaError_t e = cudaMemsetAsync(lookback, 0, sizeof(unsigned long long) * tiles, s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(ticket, 0, sizeof(uint32_t), s);
+    if (e != cudaSuccess) return e;
+    k_mark<<<tiles, kMarkThreads, 0, s>>>(P, identity ? 1u : 0u, PK, NK, n, passes, a_key, a_val, b_key, b_val, hist,
+                                          lookback, ticket, tiles, counts, err);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_merge(cudaStream_t s, const uint32_t* a_key, const uint32_t* a_val, const uint32_t* b_key,
+                         const uint32_t* b_val, const uint32_t* counts, uint32_t* split, uint32_t n,
+                         uint32_t* out_key, uint32_t* out_val, const float2* pos, float2* sorted_pos,
+                         uint32_t* kstart, uint32_t num_keys, uint4* chunks, uint32_t* chunk_count, uint32_t* err,
+                         uint32_t* kernels) {
+    if (kernels) *kernels = 0;
+    if (n == 0 || num_keys == 0) return cudaSuccess;
+    const uint32_t tiles = merge_tiles(n);
+    const uint32_t cap = kstart_chunk_cap(num_keys);
+    k_merge_path<<<(tiles + 1u + 255u) / 256u, 256, 0, s>>>(a_key, b_key, counts, n, tiles + 1u, split);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaMemsetAsync(chunk_count, 0, sizeof(uint32_t), s);
+    if (e != cudaSuccess) return e;
+    k_merge<<<tiles, kMergeThreads, 0, s>>>(a_key, a_val, b_key, b_val, counts, split, n, out_key, out_val, pos,
+                                            sorted_pos, kstart, num_keys, chunks, chunk_count, cap, err);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    k_kstart_fill<<<4 * (sms > 0 ? sms : 1), 256, 0, s>>>(chunks, chunk_count, cap, kstart);
+    if (kernels) *kernels = 3;
     return cudaGetLastError();
 }
 

@@ -51,7 +51,7 @@ cudaError_t launch_hist_scan(cudaStream_t s, const uint32_t* hist, uint32_t* off
 cudaError_t launch_onesweep(cudaStream_t s, const uint32_t* keys_in, const uint32_t* vals_in,
                             uint32_t* keys_out, uint32_t* vals_out, uint32_t n, uint32_t shift,
                             const uint32_t* digit_offset, uint32_t* lookback, uint32_t* ticket,
-                            uint32_t* err);
+                            uint32_t* err, const uint32_t* n_dev = nullptr);  // n_dev: count on the device (<= n)
 cudaError_t launch_ranges(cudaStream_t s, const uint32_t* sorted_key, uint32_t n, uint2* ranges, uint32_t num_keys,
                           uint32_t ybits = 0);
 // Key-start table of sorted keys (num_keys + 1 entries).  chunks / chunk_count
@@ -67,6 +67,21 @@ cudaError_t launch_kstart(cudaStream_t s, const uint32_t* sorted_key, uint32_t n
 cudaError_t launch_query(cudaStream_t s, uint32_t cap, const uint32_t* kstart, const uint32_t* sorted_slot,
                          const float2* sorted_pos, const uint32_t* slot_id, TileGrid grid, uint32_t n, uint32_t* count,
                          uint32_t* list, unsigned long long* pair_bins);  // pair_bins: kPairBins counters
+// Incremental index update: split the previous sorted order P (keys PK; P[q] = q when
+// identity) by whether the new key NK[slot] changed (A: unchanged, B: changed; counts
+// -> counts[0..1]; B's digit counts -> hist), then, after B is sorted, merge A and B
+// into out_key / out_val, writing the key-start table and the sorted positions.
+uint32_t mark_tiles(uint32_t n);
+uint32_t merge_tiles(uint32_t n);
+cudaError_t launch_mark(cudaStream_t s, const uint32_t* P, bool identity, const uint32_t* PK, const uint32_t* NK,
+                        uint32_t n, uint32_t passes, uint32_t* a_key, uint32_t* a_val, uint32_t* b_key,
+                        uint32_t* b_val, uint32_t* hist, unsigned long long* lookback, uint32_t* ticket,
+                        uint32_t* counts, uint32_t* err);
+cudaError_t launch_merge(cudaStream_t s, const uint32_t* a_key, const uint32_t* a_val, const uint32_t* b_key,
+                         const uint32_t* b_val, const uint32_t* counts, uint32_t* split, uint32_t n,
+                         uint32_t* out_key, uint32_t* out_val, const float2* pos, float2* sorted_pos,
+                         uint32_t* kstart, uint32_t num_keys, uint4* chunks, uint32_t* chunk_count, uint32_t* err,
+                         uint32_t* kernels);
 cudaError_t launch_iota(cudaStream_t s, uint32_t* out, uint32_t n);
 // *first_bad = first i with (head[i] & road mask) >= num_roads, or 0xffffffff
 cudaError_t launch_check_roads(cudaStream_t s, const uint32_t* head, uint32_t n, uint32_t num_roads,

@@ -92,26 +92,14 @@ constexpr uint32_t kGapDirect = 8;
 constexpr uint32_t kGapWarp = 256;
 constexpr uint32_t kGapChunk = 4096;
 
-__global__ __launch_bounds__(256) void k_kstart_pos(const uint32_t* __restrict__ sk, uint32_t n,
-                                                    uint32_t* __restrict__ kstart, uint32_t num_keys,
-                                                    uint4* __restrict__ chunks, uint32_t* chunk_count,
-                                                    uint32_t chunk_cap, const uint32_t* __restrict__ sv,
-                                                    const float2* __restrict__ pos, float2* __restrict__ sorted_pos) {
+// Writes kstart[from + r] = value for r < len, for every lane of the warp (all lanes
+// call it; a lane with nothing to write passes len = 0).
+__device__ __forceinline__ void fill_key_gaps(uint32_t from, uint32_t len, uint32_t value, uint32_t lane,
+                                              uint32_t* __restrict__ kstart, uint4* __restrict__ chunks,
+                                              uint32_t* chunk_count, uint32_t chunk_cap) {
     constexpr uint32_t FULL = 0xffffffffu;
-    const uint32_t lane = threadIdx.x & 31;
-    const uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
-    if (sorted_pos && q < n) {  // positions in sorted order, for the query's candidate reads
-        const uint32_t slot = sv[q];
-        sorted_pos[q] = slot < n ? pos[slot] : make_float2(__int_as_float(0x7fffffff), __int_as_float(0x7fffffff));
-    }
-    uint32_t from = 0, len = 0;
-    if (q <= n) {
-        from = q ? clamped_key(sk, q - 1u, num_keys) + 1u : 0u;
-        const uint32_t to = q < n ? clamped_key(sk, q, num_keys) : num_keys;  // inclusive
-        len = to >= from ? to - from + 1u : 0u;
-    }
     if (len <= kGapDirect) {
-        for (uint32_t r = 0; r < len; r++) kstart[from + r] = q;
+        for (uint32_t r = 0; r < len; r++) kstart[from + r] = value;
     }
     // medium gaps: the warp writes them together
     const uint32_t wlen = len > kGapDirect && len <= kGapWarp ? len : 0u;
@@ -134,8 +122,8 @@ __global__ __launch_bounds__(256) void k_kstart_pos(const uint32_t* __restrict__
             }
             const uint32_t o_excl = __shfl_sync(FULL, excl, owner);
             const uint32_t o_from = __shfl_sync(FULL, from, owner);
-            const uint32_t o_q = __shfl_sync(FULL, q, owner);
-            if (i < total) kstart[o_from + (i - o_excl)] = o_q;
+            const uint32_t o_val = __shfl_sync(FULL, value, owner);
+            if (i < total) kstart[o_from + (i - o_excl)] = o_val;
         }
     }
     // long gaps: chunks, one list append per warp
@@ -153,15 +141,36 @@ __global__ __launch_bounds__(256) void k_kstart_pos(const uint32_t* __restrict__
         base = __shfl_sync(FULL, base, 31) + (incl - m);
         if (m) {
             if (base + m > chunk_cap) {  // unreachable: chunk_cap bounds every key space; stay correct anyway
-                for (uint32_t r = 0; r < len; r++) kstart[from + r] = q;
+                for (uint32_t r = 0; r < len; r++) kstart[from + r] = value;
             } else {
                 for (uint32_t c = 0; c < m; c++) {
                     const uint32_t off = c * kGapChunk;
-                    chunks[base + c] = make_uint4(from + off, len - off < kGapChunk ? len - off : kGapChunk, q, 0u);
+                    chunks[base + c] =
+                        make_uint4(from + off, len - off < kGapChunk ? len - off : kGapChunk, value, 0u);
                 }
             }
         }
     }
+}
+
+__global__ __launch_bounds__(256) void k_kstart_pos(const uint32_t* __restrict__ sk, uint32_t n,
+                                                    uint32_t* __restrict__ kstart, uint32_t num_keys,
+                                                    uint4* __restrict__ chunks, uint32_t* chunk_count,
+                                                    uint32_t chunk_cap, const uint32_t* __restrict__ sv,
+                                                    const float2* __restrict__ pos, float2* __restrict__ sorted_pos) {
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (sorted_pos && q < n) {  // positions in sorted order, for the query's candidate reads
+        const uint32_t slot = sv[q];
+        sorted_pos[q] = slot < n ? pos[slot] : make_float2(__int_as_float(0x7fffffff), __int_as_float(0x7fffffff));
+    }
+    uint32_t from = 0, len = 0;
+    if (q <= n) {
+        from = q ? clamped_key(sk, q - 1u, num_keys) + 1u : 0u;
+        const uint32_t to = q < n ? clamped_key(sk, q, num_keys) : num_keys;  // inclusive
+        len = to >= from ? to - from + 1u : 0u;
+    }
+    fill_key_gaps(from, len, q, lane, kstart, chunks, chunk_count, chunk_cap);
 }
 
 __global__ __launch_bounds__(256) void k_kstart_fill(const uint4* __restrict__ chunks,
