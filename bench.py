@@ -59,7 +59,11 @@ def b_nbr(k_mean: float) -> float:
 KERNEL_BYTES = {
     "k_step": lambda k: B_STEP + 4,        # move + key write
     "k_onesweep": lambda k: 16,            # (key, id) read + write
-    "k_kstart": lambda k: 4,               # sorted key read (+ 4 B per key slot, added below)
+    "k_kstart": lambda k: 4 + 20,          # sorted key read, slot read + position gather + write
+                                           # (+ 4 B per key slot, added below)
+    "k_mark": lambda k: 20,                # previous order 4 + old key 4 + new key 4, split write 8
+    "k_merge": lambda k: 32,               # split read 8, sorted key+slot write 8, position gather 8 + write 8
+                                           # (+ 4 B per key slot, added below)
     "k_query": lambda k: 12 + 4 * k,       # own pos 8 + count 4 + kept ids
     "k_permute": lambda k: 72,             # 36-byte state read + write
     "k_step_multi": lambda k: B_STEP,      # per tick
@@ -229,7 +233,7 @@ def run_ours(args, cfg, world, rank, local):
             per_launch_bytes = B_STEP * n * prof_steps / v["launches"]
         else:
             per_launch_bytes = KERNEL_BYTES.get(name, lambda k: 0)(k_mean) * n
-            if name == "k_kstart":  # writes one word per key of the key space
+            if name in ("k_kstart", "k_merge"):  # write one word per key of the key space
                 per_launch_bytes += 4 * (2 ** info["key_bits"] + 1)
         kernels[name] = {"launches": v["launches"], "avg_ms": avg, "share": v["ms"] / total_ms,
                          "algo_bytes_per_launch": per_launch_bytes,

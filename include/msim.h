@@ -126,10 +126,13 @@ typedef struct msim_params {
     uint32_t flags;           /* MSIM_PARAM_* bits */
 } msim_params;
 
-/* msim_params.flags: rebuild the index by a full radix sort every neighbour tick
- * instead of updating the previous order (same results; for entities that move far
- * between ticks, where most keys change). */
+/* msim_params.flags: how neighbour ticks rebuild the index (same results either way).
+ * By default the previous order is updated (only entries whose key changed are
+ * sorted and merged back) from 4,000,000 entities on, and fully re-sorted below.
+ * FULL_SORT: always a full radix sort (e.g. entities that move far between ticks);
+ * INCREMENTAL: always the update. */
 #define MSIM_PARAM_FULL_SORT 1u
+#define MSIM_PARAM_INCREMENTAL 2u
 
 typedef struct msim_init {
     uint64_t seed;

@@ -147,14 +147,15 @@ class Simulation:
 
     def __init__(self, road_map: RoadMap, num_entities: int, *, rng: str = "xorshift128", dt: float = 1.0,
                  radius: float = 10.0, cap: int = 64, cell_size: float = 0.0, resort_interval: int = 0,
-                 full_sort: bool = False):
+                 index: str = "auto"):
         self.map = road_map
         self.n = int(num_entities)
         self.cap = int(cap)
         self.rng_kind = _RNG_KINDS[rng]
         p = _capi.MsimParams(num_entities=self.n, rng_kind=self.rng_kind, dt=dt, radius=radius, cap=self.cap,
                              cell_size=cell_size, resort_interval=resort_interval,
-                             flags=_capi.PARAM_FULL_SORT if full_sort else 0)
+                             flags={"auto": 0, "full": _capi.PARAM_FULL_SORT,
+                                    "incremental": _capi.PARAM_INCREMENTAL}[index])
         self._ctx = ctypes.c_void_p()
         v = road_map.view()
         check(lib().msim_create(ctypes.byref(v), ctypes.byref(p), ctypes.byref(self._ctx)))

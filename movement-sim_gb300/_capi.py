@@ -27,6 +27,7 @@ PLACE_ROAD_START = 0
 PLACE_UNIFORM_FRACTION = 1
 STEP_NEIGHBOURS = 1
 PARAM_FULL_SORT = 1
+PARAM_INCREMENTAL = 2
 NO_NEIGHBOUR = 0xFFFFFFFF
 
 

@@ -465,7 +465,9 @@ int msim_create(const msim_map* map, const msim_params* params, msim_ctx** out) 
     if (!std::isfinite(p.radius) || p.radius < 0.f) return fail(MSIM_ERR_INVALID, "radius must be finite and >= 0");
     if (p.cap > kMaxCap) return fail(MSIM_ERR_INVALID, "cap must be <= " + std::to_string(kMaxCap));
     if (p.cell_size < 0.f || !std::isfinite(p.cell_size)) return fail(MSIM_ERR_INVALID, "cell_size must be >= 0");
-    if (p.flags & ~MSIM_PARAM_FULL_SORT) return fail(MSIM_ERR_INVALID, "unknown params flags");
+    if (p.flags & ~(MSIM_PARAM_FULL_SORT | MSIM_PARAM_INCREMENTAL)) return fail(MSIM_ERR_INVALID, "unknown params flags");
+    if ((p.flags & MSIM_PARAM_FULL_SORT) && (p.flags & MSIM_PARAM_INCREMENTAL))
+        return fail(MSIM_ERR_INVALID, "MSIM_PARAM_FULL_SORT and MSIM_PARAM_INCREMENTAL exclude each other");
 
     msim_ctx* c = new (std::nothrow) msim_ctx();
     if (!c) return fail(MSIM_ERR_NOMEM, "out of host memory");
@@ -475,7 +477,9 @@ int msim_create(const msim_map* map, const msim_params* params, msim_ctx** out) 
         return cuda_fail(e, "cudaGetDevice");
     }
     c->params = p;
-    c->incremental = (p.flags & MSIM_PARAM_FULL_SORT) == 0;
+    // the incremental index update pays off from a few million entities on
+    c->incremental = (p.flags & MSIM_PARAM_FULL_SORT) == 0 &&
+                     ((p.flags & MSIM_PARAM_INCREMENTAL) != 0 || p.num_entities >= 4000000u);
     c->n = p.num_entities;
     c->R = map->num_roads;
     c->C = map->num_connections;
@@ -503,8 +507,11 @@ int msim_create(const msim_map* map, const msim_params* params, msim_ctx** out) 
     const double reach = radius * (1.0 + 0x1p-20) + maxc * 0x1p-20 + 1e-30;
     double cell = p.cell_size;
     if (cell <= 0.0) {
+        // about four entities per tile at uniform density (entities on roads bunch up
+        // more); with the bands below, the 24-bit key budget gives the fewest
+        // candidates per query around this size on lattice road networks
         double area = (double)c->world_w * (double)c->world_h;
-        cell = std::max(2.0 * reach, 4.0 * std::sqrt(area / std::max<double>(c->n, 1.0)));
+        cell = std::max(2.0 * reach, 2.0 * std::sqrt(area / std::max<double>(c->n, 1.0)));
     }
     cell = std::max(cell, 1e-3);
     uint32_t bits = 1;
@@ -527,8 +534,12 @@ int msim_create(const msim_map* map, const msim_params* params, msim_ctx** out) 
     c->grid.reach = (float)reach;
     c->grid.radius = p.radius;
     c->grid.d2_limit = sqrt_limit(p.radius);
-    // y bands inside a tile fill the key up to 24 bits (3 radix passes), at most 64 bands
-    c->grid.ybits = std::min<uint32_t>(6u, 24u - 2u * bits);
+    // y bands inside a tile fill the key up to 24 bits (3 radix passes), at most 64
+    // bands, and keep the key-start table within about four entries per entity
+    uint32_t nbits = 0;
+    while (nbits < 31u && (1ull << (nbits + 1)) <= 4ull * std::max<uint64_t>(c->n, 1)) nbits++;
+    const uint32_t budget = nbits > 2u * bits ? nbits - 2u * bits : 0u;
+    c->grid.ybits = std::min<uint32_t>(std::min<uint32_t>(6u, 24u - 2u * bits), budget);
     c->grid.ybands = (float)(1u << c->grid.ybits);
     c->passes = (2 * bits + c->grid.ybits + 7) / 8;
     c->num_keys = (size_t)1 << (2 * bits + c->grid.ybits);

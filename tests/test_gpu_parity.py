@@ -61,16 +61,16 @@ def test_plain_config_1000_ticks(msim, orc, rng_name, rng_kind):
     assert np.any(rng != _oracle_state(orc, road_map, n, rng_kind, 20261203, 1, (1.0, 1.6))[2])
 
 
-@pytest.mark.parametrize("rng_name,rng_kind,resort,full_sort",
-                         [("pcg32", 1, 3, False), ("xorshift128", 0, 1, False), ("pcg32", 1, 1000, False),
-                          ("pcg32", 1, 3, True), ("xorshift128", 0, 1000, True)])
-def test_neighbour_ticks_every_tick(msim, orc, rng_name, rng_kind, resort, full_sort):
+@pytest.mark.parametrize("rng_name,rng_kind,resort,index",
+                         [("pcg32", 1, 3, "incremental"), ("xorshift128", 0, 1, "incremental"),
+                          ("pcg32", 1, 1000, "incremental"), ("pcg32", 1, 3, "full"), ("xorshift128", 0, 1000, "auto")])
+def test_neighbour_ticks_every_tick(msim, orc, rng_name, rng_kind, resort, index):
     """Move + index + neighbour query, compared every tick (states, counts, id lists);
     the index updated from the previous order, or fully re-sorted every tick."""
     road_map = msim.RoadMap.lattice(20, 5)
     n, ticks, cap, radius = 12_345, 40, 64, 2.0
     with msim.Simulation(road_map, n, rng=rng_name, dt=0.1, radius=radius, cap=cap, resort_interval=resort,
-                         full_sort=full_sort) as sim:
+                         index=index) as sim:
         sim.init_entities(7, placement="fraction", speed=(1.0, 1.6))
         pos, head, rng, speed = _oracle_state(orc, road_map, n, rng_kind, 7, 1, (1.0, 1.6))
         for t in range(ticks):
