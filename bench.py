@@ -70,6 +70,13 @@ KERNEL_BYTES = {
     "k_hist_scan": lambda k: 0,
 }
 
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per entity and launch of
+# one ncu capture per workload (profiles/*_ncu.md); scaled by the entities of the run
+NCU_DRAM_BYTES_PER_ENTITY = {
+    "scale": {},
+    "neighbours": {},
+}
+
 
 def peaks():
     p = ROOT / "MEASURED_PEAKS.json"
@@ -223,14 +230,20 @@ def run_ours(args, cfg, world, rank, local):
     prof_steps = max(1, min(args.steps, 50))
     tick(prof_steps)
     stats = sim.kernel_stats()
+    sort = sim.sort_stats()
     sim.set_profiling(False)
     total_ms = sum(v["ms"] for v in stats.values()) or 1.0
     peak, peak_kind = peaks()
+    # entries per radix pass: n for a full sort, the entries whose key changed for an
+    # incremental update (every pass of an update sorts the same entries)
+    sorted_per_update = sort["sorted_entries"] / sort["index_updates"] if sort["index_updates"] else float(n)
     kernels = {}
     for name, v in stats.items():
         avg = v["ms"] / v["launches"]
         if name == "k_step_multi":  # several ticks per launch
             per_launch_bytes = B_STEP * n * prof_steps / v["launches"]
+        elif name == "k_onesweep":
+            per_launch_bytes = KERNEL_BYTES[name](k_mean) * sorted_per_update
         else:
             per_launch_bytes = KERNEL_BYTES.get(name, lambda k: 0)(k_mean) * n
             if name in ("k_kstart", "k_merge"):  # write one word per key of the key space
@@ -240,11 +253,9 @@ def run_ours(args, cfg, world, rank, local):
                          "achieved_gbs": per_launch_bytes / (avg / 1e3) / 1e9 if avg > 0 else None}
     dominant = max(kernels.items(), key=lambda kv: kv[1]["share"])
     traffic = None
-    tfile = ROOT / "profiles" / "ncu_traffic.json"
-    if tfile.exists():
-        t = json.loads(tfile.read_text()).get(args.config, {}).get(dominant[0])
-        if t is not None:
-            traffic = t["bytes_per_entity"] * n
+    per_entity = NCU_DRAM_BYTES_PER_ENTITY.get(args.config, {}).get(dominant[0])
+    if per_entity is not None and not any(getattr(args, k) is not None for k in ("entities", "lattice", "cap")):
+        traffic = round(per_entity * n)
     ach = dominant[1]["achieved_gbs"] or 0.0
     roofline = {"bound": "hbm", "kernel": dominant[0], "achieved": round(ach, 1), "peak": peak, "unit": "GB/s",
                 "frac": round(ach / peak, 4), "traffic": traffic, "peak_source": peak_kind}
@@ -267,10 +278,16 @@ def run_ours(args, cfg, world, rank, local):
         "value": value, "ms_per_step": ms_max / args.steps, "clocks": clocks.summary(), "k_mean": k_mean,
         "roofline": roofline, "roofline_tick": roofline_tick, "kernels": kernels, "e2e": e2e, "cpu": cpu,
         "launches": launches, "info": info, "roads": road_map.num_roads,
+        "sorted_fraction": sorted_per_update / max(n, 1),
     }
 
 
 def run_e2e(pkg, sim, cfg, n, nbr, world, steps):
+    """End to end through the C ABI with the entity state on the host (page-locked):
+    every step uploads the state, runs one tick and reads back the moved state and
+    the neighbour counts.  Headline path: msim_tick_host (one call; chunked upload,
+    move and download overlap).  Beside it, the same round trip through the four
+    separate calls (msim_set_entities, msim_step, msim_get_state, msim_get_neighbours)."""
     pos = pkg.PinnedBuffer((n, 2), np.float32)
     head = pkg.PinnedBuffer(n, np.uint32)
     rng = pkg.PinnedBuffer((n, 4), np.uint32)
@@ -284,27 +301,38 @@ def run_e2e(pkg, sim, cfg, n, nbr, world, steps):
     f32 = lambda b: b.array.ctypes.data_as(pkg._capi.f32p)  # noqa: E731
     flags = pkg._capi.STEP_NEIGHBOURS if nbr else 0
 
-    def one():
+    def fused():  # the state arrays are both input and output (a chunk is read before it is written)
+        pkg.check(L.msim_tick_host(ctx, f32(pos), u32(head), u32(rng), f32(speed), flags, f32(pos), u32(head),
+                                   u32(rng), u32(cnt) if nbr else None, None))
+
+    def separate():
         pkg.check(L.msim_set_entities(ctx, f32(pos), u32(head), u32(rng), f32(speed)))
         pkg.check(L.msim_step(ctx, 1, flags))
         pkg.check(L.msim_get_state(ctx, f32(pos), u32(head), u32(rng), None))
         if nbr:
             pkg.check(L.msim_get_neighbours(ctx, u32(cnt), None))
 
-    one()
-    barrier_sync(world)
-    t0 = time.perf_counter()
-    for _ in range(steps):
-        one()
-    barrier_sync(world)
-    dt = max_over_ranks(time.perf_counter() - t0, world)
+    def timed(fn):
+        fn()
+        barrier_sync(world)
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            fn()
+        barrier_sync(world)
+        return max_over_ranks(time.perf_counter() - t0, world)
+
+    dt = timed(fused)
+    dt_sep = timed(separate)
     h2d = n * (8 + 4 + 16 + 4)
     d2h = n * (8 + 4 + 16 + (4 if nbr else 0))
     for b in (pos, head, rng, speed, cnt):
         b.free()
     return {"value": world * n * steps / dt, "unit": "entity-steps/s", "h2d_bytes_per_step": h2d,
-            "d2h_bytes_per_step": d2h, "steps": steps,
-            "path": "msim_set_entities (pinned host) + msim_step(1) + msim_get_state + msim_get_neighbours(counts)"}
+            "d2h_bytes_per_step": d2h, "steps": steps, "ms_per_step": 1e3 * dt / steps,
+            "path": "msim_tick_host: page-locked host state in and out (pos, heading, rng, speed in; pos, heading, "
+                    "rng, neighbour counts out)",
+            "separate_calls": {"value": world * n * steps / dt_sep, "ms_per_step": 1e3 * dt_sep / steps,
+                               "path": "msim_set_entities + msim_step(1) + msim_get_state + msim_get_neighbours"}}
 
 
 def run_batched(args, world, rank, local):
@@ -687,6 +715,7 @@ def main():
         config["sort_passes"] = r["info"]["sort_passes"]
         config["resort_interval"] = r["info"]["resort_interval"]
         config["mean_kept_neighbours"] = round(r["k_mean"], 4)
+        config["sorted_fraction_per_tick"] = round(r["sorted_fraction"], 5)
         line.update({"value": r["value"], "ms_per_step": r["ms_per_step"], "roofline": r["roofline"],
                      "roofline_tick": r["roofline_tick"], "cpu_baseline": r["cpu"], "e2e": r["e2e"],
                      "clocks": r["clocks"], "gpu_launches": r["launches"],

@@ -157,7 +157,10 @@ int msim_init_entities(msim_ctx* ctx, const msim_init* init);
 
 /* Replaces the host->device upload of the entity buffer (Simulator.cpp:189-193).
  * pos: 2N floats, heading: N words, rng: 4N words, speed: N floats (speed may be
- * NULL for 1.4 m per tick at dt = 1).  Builds the tick-0 index. */
+ * NULL for 1.4 m per tick at dt = 1).  The state stays in the caller's entity order;
+ * the next neighbour tick builds the index with a full sort and the tick after it
+ * re-orders the state spatially, so a caller that sets the state before every tick
+ * pays no re-ordering. */
 int msim_set_entities(msim_ctx* ctx, const float* pos, const uint32_t* heading,
                       const uint32_t* rng, const float* speed);
 
@@ -183,6 +186,26 @@ int msim_get_state(msim_ctx* ctx, float* pos, uint32_t* heading, uint32_t* rng, 
  * idx (N*cap words, may be NULL) holds the min(count, cap) smallest such j in
  * ascending order, the rest MSIM_NO_NEIGHBOUR.  Synchronous. */
 int msim_get_neighbours(msim_ctx* ctx, uint32_t* count, uint32_t* idx);
+
+/* One tick with the entity state on the host: the same results as
+ * msim_set_entities(in_*), msim_step(ctx, 1, flags), msim_get_state(out_*) and,
+ * with MSIM_STEP_NEIGHBOURS, msim_get_neighbours(out_count, out_idx) in a row.
+ * Replaces one Simulator::sim_tick (Simulator.cpp:213-279: the move and collision
+ * dispatches, then the entity readback of :248-263) for a caller that owns the state
+ * on the host and uploads it first (Simulator.cpp:189-193).  The entities go in
+ * chunks of at least 65,536 (up to 8): a chunk is moved as soon as it has arrived and
+ * downloaded while later chunks still upload, so the two copy directions overlap;
+ * the index and the query follow once every chunk has moved.  With page-locked host
+ * buffers (msim_host_alloc) the copies run asynchronously; pageable ones work too.
+ * in_speed may be NULL (1.4 m per tick at dt = 1); any output may be NULL; out_count
+ * and out_idx need MSIM_STEP_NEIGHBOURS.  in_pos / out_pos (and heading, rng) may be
+ * the same arrays: a chunk has been uploaded before its download writes it.
+ * Synchronous.  A heading naming a road out of
+ * range gives MSIM_ERR_OOB and keeps the previous state (as msim_set_entities);
+ * the outputs are then undefined. */
+int msim_tick_host(msim_ctx* ctx, const float* in_pos, const uint32_t* in_heading, const uint32_t* in_rng,
+                   const float* in_speed, uint32_t flags, float* out_pos, uint32_t* out_heading,
+                   uint32_t* out_rng, uint32_t* out_count, uint32_t* out_idx);
 
 /* debugData[1] of the last neighbour tick (random_move.comp:548): pairs j < i. */
 int msim_get_collision_pairs(msim_ctx* ctx, uint64_t* pairs);
@@ -242,6 +265,11 @@ int msim_reset_kernel_stats(msim_ctx* ctx);
 int msim_get_kernel_stats(msim_ctx* ctx, uint32_t kernel, uint64_t* launches, double* total_ms);
 uint32_t msim_kernel_count(void);
 const char* msim_kernel_name(uint32_t kernel);
+/* Index updates (full sorts and incremental updates) since the stats were reset, and
+ * the entries that went through their radix passes (n per full sort, the entries
+ * whose key changed per incremental update): the sort's work per tick.
+ * Synchronises the context's stream. */
+int msim_get_sort_stats(msim_ctx* ctx, uint64_t* index_updates, uint64_t* sorted_entries);
 
 /* Events on the context's stream around a region of queued work (bench timing). */
 int msim_timer_begin(msim_ctx* ctx);

@@ -204,6 +204,32 @@ class Simulation:
     def sync(self) -> None:
         check(lib().msim_sync(self._ctx))
 
+    def tick_host(self, state: dict, neighbours: bool = True, out: dict | None = None, with_idx: bool = False):
+        """One tick with the state on the host (msim_tick_host): uploads state (pos,
+        heading, rng, optional speed), moves, [index + query], returns the moved state
+        and, with neighbours, the counts (and lists when with_idx).  `out` may supply
+        the output arrays (page-locked ones let the copies overlap)."""
+        n = self.n
+        pos = np.ascontiguousarray(state["pos"], dtype=np.float32).reshape(n, 2)
+        head = np.ascontiguousarray(state["heading"], dtype=np.uint32).reshape(n)
+        rng = np.ascontiguousarray(state["rng"], dtype=np.uint32).reshape(n, 4)
+        speed = state.get("speed")
+        if speed is not None:
+            speed = np.ascontiguousarray(speed, dtype=np.float32).reshape(n)
+        if out is None:
+            out = {"pos": np.empty((n, 2), np.float32), "heading": np.empty(n, np.uint32),
+                   "rng": np.empty((n, 4), np.uint32)}
+            if neighbours:
+                out["count"] = np.empty(n, np.uint32)
+                if with_idx and self.cap:
+                    out["idx"] = np.empty((n, self.cap), np.uint32)
+        check(lib().msim_tick_host(self._ctx, _ptr(pos, ctypes.c_float), _ptr(head, ctypes.c_uint32),
+                                   _ptr(rng, ctypes.c_uint32), _ptr(speed, ctypes.c_float),
+                                   _capi.STEP_NEIGHBOURS if neighbours else 0, _ptr(out.get("pos"), ctypes.c_float),
+                                   _ptr(out.get("heading"), ctypes.c_uint32), _ptr(out.get("rng"), ctypes.c_uint32),
+                                   _ptr(out.get("count"), ctypes.c_uint32), _ptr(out.get("idx"), ctypes.c_uint32)))
+        return out
+
     @property
     def tick(self) -> int:
         t = ctypes.c_uint64()
@@ -272,6 +298,12 @@ class Simulation:
             if n.value:
                 out[lib().msim_kernel_name(k).decode()] = {"launches": n.value, "ms": ms.value}
         return out
+
+    def sort_stats(self) -> dict:
+        """Index updates since the stats were reset and the entries their radix passes sorted."""
+        u, e = ctypes.c_uint64(), ctypes.c_uint64()
+        check(lib().msim_get_sort_stats(self._ctx, ctypes.byref(u), ctypes.byref(e)))
+        return {"index_updates": u.value, "sorted_entries": e.value}
 
     def timer_begin(self) -> None:
         check(lib().msim_timer_begin(self._ctx))

@@ -40,6 +40,10 @@ static const char* const kKernelNames[K_COUNT] = {"k_init",   "k_step",    "k_st
                                                   "k_onesweep", "k_kstart", "k_query",     "k_permute",
                                                   "k_export", "k_mark",    "k_merge"};
 
+// msim_tick_host: at most this many chunks, each at least kHostChunkMin entities
+constexpr uint32_t kHostChunks = 8;
+constexpr uint32_t kHostChunkMin = 65536;
+
 }  // namespace msim
 
 using namespace msim;
@@ -87,6 +91,11 @@ struct msim_ctx {
     unsigned long long* mark_lookback = nullptr;
     uint32_t* mark_ticket = nullptr;
     uint32_t* merge_split = nullptr;
+    // entries that went through the radix passes since the stats were reset: full
+    // sorts counted on the host, incremental updates' changed entries on the device
+    unsigned long long* sorted_dev = nullptr;
+    uint64_t sorted_host = 0;
+    uint64_t index_updates = 0;
     // neighbours
     uint32_t* nbr_count = nullptr;
     uint32_t* nbr_list = nullptr;
@@ -122,6 +131,11 @@ struct msim_ctx {
     cudaEvent_t ev_index = nullptr;  // key-start table and sorted positions of tick t ready
     cudaEvent_t ev_query = nullptr;  // query of tick t done
     bool query_pending = false;
+    // host round trip (msim_tick_host): upload and download streams, per-chunk events
+    cudaStream_t up = nullptr, down = nullptr;
+    cudaEvent_t ev_start = nullptr;
+    cudaEvent_t ev_up[kHostChunks] = {};
+    cudaEvent_t ev_moved[kHostChunks] = {};
 
     DeviceMap dmap() const {
         DeviceMap m;
@@ -181,6 +195,13 @@ void free_all(msim_ctx* c) {
     if (c->ev_index) cudaEventDestroy(c->ev_index);
     if (c->ev_query) cudaEventDestroy(c->ev_query);
     if (c->qstream) cudaStreamDestroy(c->qstream);
+    if (c->ev_start) cudaEventDestroy(c->ev_start);
+    for (uint32_t k = 0; k < kHostChunks; k++) {
+        if (c->ev_up[k]) cudaEventDestroy(c->ev_up[k]);
+        if (c->ev_moved[k]) cudaEventDestroy(c->ev_moved[k]);
+    }
+    if (c->up) cudaStreamDestroy(c->up);
+    if (c->down) cudaStreamDestroy(c->down);
     if (c->stream) cudaStreamDestroy(c->stream);
 }
 
@@ -273,6 +294,8 @@ int join_query(msim_ctx* c) {
     return MSIM_OK;
 }
 
+int sort_keys(msim_ctx* c);
+
 // key + histogram (of the current positions, or after one move tick) + radix sort
 int sort_entities(msim_ctx* c, uint32_t move_ticks) {
     CK(cudaMemsetAsync(c->hist, 0, sizeof(uint32_t) * kMaxPasses * kRadix, c->stream), "memset hist");
@@ -280,6 +303,11 @@ int sort_entities(msim_ctx* c, uint32_t move_ticks) {
         Prof p(c, K_STEP);
         CK(launch_step(c->stream, step_args(c, move_ticks, true)), "k_step");
     }
+    return sort_keys(c);
+}
+
+// radix sort of (key, slot) for keys and digit counts already in c->key / c->hist
+int sort_keys(msim_ctx* c) {
     {
         Prof p(c, K_HIST_SCAN);
         CK(launch_hist_scan(c->stream, c->hist, c->digit_off, c->passes), "k_hist_scan");
@@ -301,6 +329,8 @@ int sort_entities(msim_ctx* c, uint32_t move_ticks) {
     c->sorted_key = c->sk[(c->passes - 1) & 1];
     c->sorted_slot = c->sv[(c->passes - 1) & 1];
     c->have_sort = true;
+    c->sorted_host += c->n;
+    c->index_updates++;
     return MSIM_OK;
 }
 
@@ -312,6 +342,17 @@ int permute_state(msim_ctx* c) {
     c->order_identity = true;  // slot q now holds the entity at sorted position q
     c->since_permute = 0;
     return MSIM_OK;
+}
+
+// Forget the index (new entity state in slot = id order): the next neighbour tick
+// runs a full sort, and the one after re-orders the state by it.
+void reset_index(msim_ctx* c) {
+    c->have_nbr = false;
+    c->have_sort = false;
+    c->sorted_key = nullptr;
+    c->sorted_slot = nullptr;
+    c->order_identity = false;
+    c->since_permute = c->resort;
 }
 
 // tick-0 index: the reference's first dispatch only inserts every entity into its
@@ -339,8 +380,9 @@ int incremental_index(msim_ctx* c) {
         Prof p(c, K_MARK);
         CK(launch_mark(c->stream, c->sorted_slot, c->order_identity, c->sorted_key, c->key, c->n, c->passes,
                        c->a_key, c->a_val, c->b_key[0], c->b_val[0], c->hist, c->mark_lookback, c->mark_ticket,
-                       c->ab_counts, c->err),
+                       c->ab_counts, c->err, c->sorted_dev),
            "k_mark");
+        c->index_updates++;
     }
     {
         Prof p(c, K_HIST_SCAN);
@@ -377,6 +419,9 @@ int incremental_index(msim_ctx* c) {
     return MSIM_OK;
 }
 
+int key_start_table(msim_ctx* c);
+int run_query(msim_ctx* c, bool overlap);
+
 int neighbour_tick(msim_ctx* c) {
     int rc;
     if (c->have_sort && c->since_permute >= c->resort) {
@@ -389,19 +434,31 @@ int neighbour_tick(msim_ctx* c) {
     } else {
         rc = sort_entities(c, 1);
         if (rc != MSIM_OK) return rc;
-        c->order_identity = false;
-        Prof p(c, K_KSTART);
-        uint32_t launched = 0;
-        CK(launch_kstart(c->stream, c->sorted_key, c->n, c->kstart, (uint32_t)c->num_keys, c->kstart_chunks,
-                         c->kstart_chunk_count, &launched, c->sorted_slot, cur_state(c).pos, c->sorted_pos),
-           "k_kstart");
-        if (launched > 1) c->launch_count += launched - 1;
+        rc = key_start_table(c);
+        if (rc != MSIM_OK) return rc;
     }
+    return run_query(c, true);
+}
+
+// key-start table and positions in sorted order, after a full sort
+int key_start_table(msim_ctx* c) {
+    c->order_identity = false;
+    Prof p(c, K_KSTART);
+    uint32_t launched = 0;
+    CK(launch_kstart(c->stream, c->sorted_key, c->n, c->kstart, (uint32_t)c->num_keys, c->kstart_chunks,
+                     c->kstart_chunk_count, &launched, c->sorted_slot, cur_state(c).pos, c->sorted_pos),
+       "k_kstart");
+    if (launched > 1) c->launch_count += launched - 1;
+    return MSIM_OK;
+}
+
+// The radius query over the index just built.
+int run_query(msim_ctx* c, bool overlap) {
     // The query reads only the index (key-start table, sorted slots and positions)
     // and slot ids: the next tick's move step may overwrite positions meanwhile.  With
     // profiling on everything stays on one stream so the kernel times do not overlap.
     cudaStream_t qs = c->stream;
-    if (!c->profiling) {
+    if (overlap && !c->profiling) {
         CK(cudaEventRecord(c->ev_index, c->stream), "cudaEventRecord");
         CK(cudaStreamWaitEvent(c->qstream, c->ev_index, 0), "cudaStreamWaitEvent");
         qs = c->qstream;
@@ -567,7 +624,7 @@ int msim_create(const msim_map* map, const msim_params* params, msim_ctx** out) 
         (rc = dalloc(c, &c->b_key[0], n)) || (rc = dalloc(c, &c->b_key[1], n)) || (rc = dalloc(c, &c->b_val[0], n)) ||
         (rc = dalloc(c, &c->b_val[1], n)) || (rc = dalloc(c, &c->ab_counts, 2)) ||
         (rc = dalloc(c, &c->mark_lookback, mark_tiles(c->n))) || (rc = dalloc(c, &c->mark_ticket, 1)) ||
-        (rc = dalloc(c, &c->merge_split, (size_t)merge_tiles(c->n) + 1)) ||
+        (rc = dalloc(c, &c->merge_split, (size_t)merge_tiles(c->n) + 1)) || (rc = dalloc(c, &c->sorted_dev, 1)) ||
         (rc = dalloc(c, &c->nbr_count, n)) || (rc = dalloc(c, &c->pairs, kPairBins)) || (rc = dalloc(c, &c->err, 1)) ||
         (rc = dalloc(c, &c->check, 1)))
         return bail(rc);
@@ -584,6 +641,7 @@ int msim_create(const msim_map* map, const msim_params* params, msim_ctx** out) 
     if (e == cudaSuccess) e = cudaMemcpy(c->road_conn, map->road_conn, sizeof(uint4) * c->R, cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemcpy(c->conn, conn.data(), sizeof(uint32_t) * (c->C + 1), cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemsetAsync(c->err, 0, sizeof(uint32_t), c->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(c->sorted_dev, 0, sizeof(unsigned long long), c->stream);
     for (int b = 0; b < 2 && e == cudaSuccess; b++) {
         e = cudaMemsetAsync(c->st[b].pos, 0, sizeof(float2) * std::max<size_t>(n, 1), c->stream);
         if (e == cudaSuccess) e = cudaMemsetAsync(c->st[b].head, 0, sizeof(uint32_t) * std::max<size_t>(n, 1), c->stream);
@@ -652,9 +710,14 @@ int msim_set_entities(msim_ctx* c, const float* pos, const uint32_t* heading, co
                                       std::to_string(heading[first_bad] & MSIM_HEADING_ROAD_MASK) + " of " +
                                       std::to_string(c->R));
     c->cur = b;
-    // entity i starts in slot i
+    // entity i starts in slot i.  No index is built here: the next neighbour tick
+    // sorts from scratch, and re-orders the state into spatial order the tick after
+    // (a re-ordering from the caller's arbitrary order is a random gather, as costly
+    // as the upload itself; a caller that sets the state before every tick never
+    // pays it).
     CK(launch_iota(c->stream, s.slot_id, c->n), "k_iota");
-    return build_index(c);
+    reset_index(c);
+    return MSIM_OK;
 }
 
 int msim_set_road_factors(msim_ctx* c, const float* factors) {
@@ -756,6 +819,132 @@ int msim_get_neighbours(msim_ctx* c, uint32_t* count, uint32_t* idx) {
     return sync_and_check(c);
 }
 
+int msim_tick_host(msim_ctx* c, const float* in_pos, const uint32_t* in_heading, const uint32_t* in_rng,
+                   const float* in_speed, uint32_t flags, float* out_pos, uint32_t* out_heading, uint32_t* out_rng,
+                   uint32_t* out_count, uint32_t* out_idx) {
+    int rc = check_ctx(c);
+    if (rc != MSIM_OK) return rc;
+    if (flags & ~MSIM_STEP_NEIGHBOURS) return fail(MSIM_ERR_INVALID, "unknown step flags");
+    const bool nbr = (flags & MSIM_STEP_NEIGHBOURS) != 0;
+    if ((out_count || out_idx) && !nbr) return fail(MSIM_ERR_INVALID, "neighbour outputs need MSIM_STEP_NEIGHBOURS");
+    const uint32_t n = c->n;
+    if (n && (!in_pos || !in_heading || !in_rng)) return fail(MSIM_ERR_INVALID, "pos, heading and rng are required");
+    if (n == 0) {
+        c->tick++;
+        return MSIM_OK;
+    }
+    if (!c->up) {
+        CK(cudaStreamCreateWithFlags(&c->up, cudaStreamNonBlocking), "cudaStreamCreate");
+        CK(cudaStreamCreateWithFlags(&c->down, cudaStreamNonBlocking), "cudaStreamCreate");
+        CK(cudaEventCreateWithFlags(&c->ev_start, cudaEventDisableTiming), "cudaEventCreate");
+        for (uint32_t k = 0; k < kHostChunks; k++) {
+            CK(cudaEventCreateWithFlags(&c->ev_up[k], cudaEventDisableTiming), "cudaEventCreate");
+            CK(cudaEventCreateWithFlags(&c->ev_moved[k], cudaEventDisableTiming), "cudaEventCreate");
+        }
+    }
+    // The spare state buffer receives the upload; earlier work (a re-ordering that
+    // read it, a query still running) finishes first.
+    if ((rc = join_query(c)) != MSIM_OK) return rc;
+    const int old = c->cur;
+    const int b = 1 - old;
+    EntityState& s = c->st[b];
+    CK(cudaMemsetAsync(c->check, 0xff, sizeof(uint32_t), c->stream), "memset check");
+    if (nbr) CK(cudaMemsetAsync(c->hist, 0, sizeof(uint32_t) * kMaxPasses * kRadix, c->stream), "memset hist");
+    CK(cudaEventRecord(c->ev_start, c->stream), "cudaEventRecord");
+    CK(cudaStreamWaitEvent(c->up, c->ev_start, 0), "cudaStreamWaitEvent");
+
+    // chunk k: upload (up) -> check headings, move, key, digit counts (stream) ->
+    // download of the moved state (down); chunk k's download overlaps chunk k+1's upload
+    const uint32_t chunk = std::max<uint32_t>(kHostChunkMin, (n + kHostChunks - 1) / kHostChunks);
+    uint32_t k = 0;
+    for (uint32_t lo = 0; lo < n; lo += chunk, k++) {
+        const uint32_t cnt = std::min(chunk, n - lo);
+        CK(cudaMemcpyAsync(s.head + lo, in_heading + lo, sizeof(uint32_t) * cnt, cudaMemcpyHostToDevice, c->up),
+           "upload heading");
+        CK(cudaMemcpyAsync(s.pos + lo, in_pos + 2 * (size_t)lo, sizeof(float2) * cnt, cudaMemcpyHostToDevice, c->up),
+           "upload pos");
+        CK(cudaMemcpyAsync(s.rng + lo, in_rng + 4 * (size_t)lo, sizeof(uint4) * cnt, cudaMemcpyHostToDevice, c->up),
+           "upload rng");
+        if (in_speed)
+            CK(cudaMemcpyAsync(s.speed + lo, in_speed + lo, sizeof(float) * cnt, cudaMemcpyHostToDevice, c->up),
+               "upload speed");
+        CK(cudaEventRecord(c->ev_up[k], c->up), "cudaEventRecord");
+        CK(cudaStreamWaitEvent(c->stream, c->ev_up[k], 0), "cudaStreamWaitEvent");
+        if (!in_speed) CK(launch_fill(c->stream, s.speed + lo, cnt, 1.4f), "k_fill");  // SPEED, random_move.comp:750
+        CK(launch_check_roads_range(c->stream, s.head, lo, cnt, c->R, c->check), "k_check_roads");
+        {
+            Prof p(c, K_STEP);
+            StepLaunch a = step_args(c, 1, nbr);
+            a.st.pos = s.pos + lo;
+            a.st.head = s.head + lo;
+            a.st.rng = s.rng + lo;
+            a.st.speed = s.speed + lo;
+            a.st.slot_id = s.slot_id + lo;
+            a.n = cnt;
+            a.key = nbr ? c->key + lo : nullptr;
+            a.blocks = std::min<int>(c->step_blocks, (int)((cnt + kStepThreads - 1) / kStepThreads));
+            CK(launch_step(c->stream, a), "k_step");
+        }
+        CK(cudaEventRecord(c->ev_moved[k], c->stream), "cudaEventRecord");
+        CK(cudaStreamWaitEvent(c->down, c->ev_moved[k], 0), "cudaStreamWaitEvent");
+        if (out_pos)
+            CK(cudaMemcpyAsync(out_pos + 2 * (size_t)lo, s.pos + lo, sizeof(float2) * cnt, cudaMemcpyDeviceToHost,
+                               c->down),
+               "download pos");
+        if (out_heading)
+            CK(cudaMemcpyAsync(out_heading + lo, s.head + lo, sizeof(uint32_t) * cnt, cudaMemcpyDeviceToHost, c->down),
+               "download heading");
+        if (out_rng)
+            CK(cudaMemcpyAsync(out_rng + 4 * (size_t)lo, s.rng + lo, sizeof(uint4) * cnt, cudaMemcpyDeviceToHost,
+                               c->down),
+               "download rng");
+    }
+    CK(launch_iota(c->stream, s.slot_id, n), "k_iota");  // entity i in slot i
+    c->cur = b;
+    reset_index(c);
+    if (nbr) {
+        if ((rc = sort_keys(c)) != MSIM_OK || (rc = key_start_table(c)) != MSIM_OK ||
+            (rc = run_query(c, false)) != MSIM_OK)
+            return rc;
+        if (out_count || out_idx) {
+            const bool want_idx = out_idx && c->params.cap;
+            const size_t cap = c->params.cap;
+            if ((rc = ensure_stage(c, (size_t)n * sizeof(uint32_t) * (1 + (want_idx ? cap : 0)))) != MSIM_OK)
+                return rc;
+            uint32_t* d_count = static_cast<uint32_t*>(c->stage);
+            uint32_t* d_idx = want_idx ? d_count + n : nullptr;
+            {
+                Prof p(c, K_EXPORT);
+                CK(launch_export_neighbours(c->stream, c->sorted_slot, s.slot_id, c->nbr_count, c->nbr_list, n,
+                                            c->params.cap, d_count, d_idx),
+                   "k_export_nbr");
+            }
+            if (out_count)
+                CK(cudaMemcpyAsync(out_count, d_count, sizeof(uint32_t) * n, cudaMemcpyDeviceToHost, c->stream),
+                   "download counts");
+            if (want_idx)
+                CK(cudaMemcpyAsync(out_idx, d_idx, sizeof(uint32_t) * n * cap, cudaMemcpyDeviceToHost, c->stream),
+                   "download neighbours");
+        }
+    }
+    c->tick++;
+    uint32_t first_bad = 0;
+    CK(cudaMemcpyAsync(&first_bad, c->check, sizeof(first_bad), cudaMemcpyDeviceToHost, c->stream), "read check");
+    CK(cudaStreamSynchronize(c->down), "cudaStreamSynchronize");
+    CK(cudaStreamSynchronize(c->stream), "cudaStreamSynchronize");
+    if (first_bad != 0xffffffffu) {  // as msim_set_entities: the previous state stays
+        c->cur = old;
+        reset_index(c);
+        c->tick--;
+        CK(cudaMemsetAsync(c->err, 0, sizeof(uint32_t), c->stream), "clear device status");
+        CK(cudaStreamSynchronize(c->stream), "cudaStreamSynchronize");
+        return fail(MSIM_ERR_OOB, "heading of entity " + std::to_string(first_bad) + " names road " +
+                                      std::to_string(in_heading[first_bad] & MSIM_HEADING_ROAD_MASK) + " of " +
+                                      std::to_string(c->R));
+    }
+    return sync_and_check(c);
+}
+
 int msim_get_collision_pairs(msim_ctx* c, uint64_t* pairs) {
     int rc = check_ctx(c);
     if (rc != MSIM_OK) return rc;
@@ -825,7 +1014,21 @@ int msim_reset_kernel_stats(msim_ctx* c) {
         c->launches[k] = 0;
         c->ms[k] = 0.0;
     }
+    c->sorted_host = 0;
+    c->index_updates = 0;
+    CK(cudaMemsetAsync(c->sorted_dev, 0, sizeof(unsigned long long), c->stream), "memset sort stats");
     return rc;
+}
+
+int msim_get_sort_stats(msim_ctx* c, uint64_t* index_updates, uint64_t* sorted_entries) {
+    int rc = check_ctx(c);
+    if (rc != MSIM_OK) return rc;
+    unsigned long long dev = 0;
+    CK(cudaMemcpyAsync(&dev, c->sorted_dev, sizeof(dev), cudaMemcpyDeviceToHost, c->stream), "read sort stats");
+    CK(cudaStreamSynchronize(c->stream), "cudaStreamSynchronize");
+    if (index_updates) *index_updates = c->index_updates;
+    if (sorted_entries) *sorted_entries = c->sorted_host + dev;
+    return MSIM_OK;
 }
 
 int msim_get_kernel_stats(msim_ctx* c, uint32_t kernel, uint64_t* launches, double* total_ms) {

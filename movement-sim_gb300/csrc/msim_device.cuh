@@ -173,8 +173,9 @@ __host__ __device__ __forceinline__ constexpr uint32_t part1by1(uint32_t x) {
 __host__ __device__ __forceinline__ uint32_t morton2(uint32_t x, uint32_t y) {
     return part1by1(x) | (part1by1(y) << 1);
 }
-// Tile coordinates are below 2^11: their bit spreads come from a constant table
-// (lanes of a warp mostly share tiles, so the constant cache broadcasts).
+// Tile coordinates are below 2^11: their bit spreads come from a constant table.
+// For the query only, whose lanes hold consecutive sorted entries and so mostly
+// share tiles (the constant cache broadcasts); divergent indices serialise.
 struct MortonTable {
     uint32_t v[2048];
 };
@@ -213,9 +214,13 @@ __device__ __forceinline__ uint32_t y_band(const TileGrid& g, float y, uint32_t 
     if (f >= g.ybands) return (1u << g.ybits) - 1u;
     return (uint32_t)f;
 }
-__device__ __forceinline__ uint32_t tile_key(const TileGrid& g, float2 p) {
+// Sort key of a position.  mtab: the 2048 bit spreads part1by1(i), in shared
+// memory (kernels over entities in any order: lanes with different tiles cost a
+// bank conflict at worst, where the constant cache would serialise them).
+__device__ __forceinline__ uint32_t tile_key(const TileGrid& g, float2 p, const uint32_t* mtab) {
     const uint32_t ty = tile_coord(p.y, g.inv_cell, g.tiles_y);
-    const uint32_t t = morton2_tile(tile_coord(p.x, g.inv_cell, g.tiles_x), ty);
+    const uint32_t tx = tile_coord(p.x, g.inv_cell, g.tiles_x);
+    const uint32_t t = mtab[tx & 2047u] | (mtab[ty & 2047u] << 1);
     return g.ybits ? ((t << g.ybits) | y_band(g, p.y, ty)) : t;
 }
 

@@ -44,7 +44,8 @@ __global__ __launch_bounds__(kMarkThreads) void k_mark(const uint32_t* __restric
                                                        uint32_t* __restrict__ a_key, uint32_t* __restrict__ a_val,
                                                        uint32_t* __restrict__ b_key, uint32_t* __restrict__ b_val,
                                                        uint32_t* hist, unsigned long long* lookback, uint32_t* ticket,
-                                                       uint32_t num_tiles, uint32_t* counts, uint32_t* err) {
+                                                       uint32_t num_tiles, uint32_t* counts, uint32_t* err,
+                                                       unsigned long long* changed_total) {
     constexpr uint32_t FULL = 0xffffffffu;
     constexpr uint32_t NW = kMarkThreads / 32;
     __shared__ uint32_t s_key[kMarkTile], s_val[kMarkTile];  // A entries, then B entries, in q order
@@ -155,6 +156,7 @@ __global__ __launch_bounds__(kMarkThreads) void k_mark(const uint32_t* __restric
             if (tile == num_tiles - 1) {
                 counts[0] = ea + tot_a;
                 counts[1] = eb + tot_b;
+                if (changed_total) atomicAdd(changed_total, (unsigned long long)(eb + tot_b));
             }
         }
     }

@@ -143,8 +143,10 @@ __device__ __forceinline__ void digit_counts(uint32_t key, bool valid, uint32_t 
 template <int RNG, bool KEY>
 __global__ __launch_bounds__(kStepThreads) void k_step(StepLaunch a) {
     __shared__ uint32_t s_hist[kMaxPasses * kRadix];
+    __shared__ uint32_t s_morton[KEY ? 2048 : 1];
     if (KEY) {
         for (uint32_t i = threadIdx.x; i < a.passes * kRadix; i += kStepThreads) s_hist[i] = 0u;
+        for (uint32_t i = threadIdx.x; i < 2048u; i += kStepThreads) s_morton[i] = part1by1(i);
         __syncthreads();
     }
     const uint32_t lane = threadIdx.x & 31;
@@ -184,7 +186,7 @@ __global__ __launch_bounds__(kStepThreads) void k_step(StepLaunch a) {
                 if (rd) a.st.rng[sl[u]] = r;
             }
             if (KEY) {
-                key[u] = tile_key(a.grid, p[u]);
+                key[u] = tile_key(a.grid, p[u], s_morton);
                 a.key[sl[u]] = key[u];
             }
         }
@@ -565,11 +567,12 @@ __global__ void k_export_colors(const uint32_t* sorted_slot, const uint32_t* slo
 }
 
 // First entity whose heading names a road >= num_roads (atomicMin into *first_bad).
-__global__ void k_check_roads(const uint32_t* __restrict__ head, uint32_t n, uint32_t num_roads, uint32_t* first_bad) {
+__global__ void k_check_roads(const uint32_t* __restrict__ head, uint32_t n, uint32_t num_roads, uint32_t base,
+                              uint32_t* first_bad) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     const bool bad = i < n && (head[i] & kHeadRoad) >= num_roads;
     const unsigned m = __ballot_sync(0xffffffffu, bad);
-    if (m && (threadIdx.x & 31) == (uint32_t)(__ffs(m) - 1)) atomicMin(first_bad, i);
+    if (m && (threadIdx.x & 31) == (uint32_t)(__ffs(m) - 1)) atomicMin(first_bad, base + i);
 }
 
 __global__ void k_fill_f32(float* out, uint32_t n, float v) {
@@ -730,8 +733,14 @@ cudaError_t launch_query(cudaStream_t s, uint32_t cap, const uint32_t* kstart, c
 cudaError_t launch_check_roads(cudaStream_t s, const uint32_t* head, uint32_t n, uint32_t num_roads,
                                uint32_t* first_bad) {
     cudaError_t e = cudaMemsetAsync(first_bad, 0xff, sizeof(uint32_t), s);
-    if (e != cudaSuccess || n == 0) return e;
-    k_check_roads<<<blocks_for(n, 256), 256, 0, s>>>(head, n, num_roads, first_bad);
+    if (e != cudaSuccess) return e;
+    return launch_check_roads_range(s, head, 0, n, num_roads, first_bad);
+}
+
+cudaError_t launch_check_roads_range(cudaStream_t s, const uint32_t* head, uint32_t first, uint32_t n,
+                                     uint32_t num_roads, uint32_t* first_bad) {
+    if (n == 0) return cudaSuccess;
+    k_check_roads<<<blocks_for(n, 256), 256, 0, s>>>(head + first, n, num_roads, first, first_bad);
     return cudaGetLastError();
 }
 
@@ -747,14 +756,14 @@ uint32_t merge_tiles(uint32_t n) { return (n + kMergeTile - 1u) / kMergeTile; }
 cudaError_t launch_mark(cudaStream_t s, const uint32_t* P, bool identity, const uint32_t* PK, const uint32_t* NK,
                         uint32_t n, uint32_t passes, uint32_t* a_key, uint32_t* a_val, uint32_t* b_key,
                         uint32_t* b_val, uint32_t* hist, unsigned long long* lookback, uint32_t* ticket,
-                        uint32_t* counts, uint32_t* err) {
+                        uint32_t* counts, uint32_t* err, unsigned long long* changed_total) {
     if (n == 0) return cudaMemsetAsync(counts, 0, 2 * sizeof(uint32_t), s);
     const uint32_t tiles = mark_tiles(n);
     cudaError_t e = cudaMemsetAsync(lookback, 0, sizeof(unsigned long long) * tiles, s);
     if (e == cudaSuccess) e = cudaMemsetAsync(ticket, 0, sizeof(uint32_t), s);
     if (e != cudaSuccess) return e;
     k_mark<<<tiles, kMarkThreads, 0, s>>>(P, identity ? 1u : 0u, PK, NK, n, passes, a_key, a_val, b_key, b_val, hist,
-                                          lookback, ticket, tiles, counts, err);
+                                          lookback, ticket, tiles, counts, err, changed_total);
     return cudaGetLastError();
 }
 

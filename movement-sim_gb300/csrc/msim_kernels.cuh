@@ -71,12 +71,13 @@ cudaError_t launch_query(cudaStream_t s, uint32_t cap, const uint32_t* kstart, c
 // identity) by whether the new key NK[slot] changed (A: unchanged, B: changed; counts
 // -> counts[0..1]; B's digit counts -> hist), then, after B is sorted, merge A and B
 // into out_key / out_val, writing the key-start table and the sorted positions.
+// changed_total (may be NULL) accumulates |B| (entries that go through the sort).
 uint32_t mark_tiles(uint32_t n);
 uint32_t merge_tiles(uint32_t n);
 cudaError_t launch_mark(cudaStream_t s, const uint32_t* P, bool identity, const uint32_t* PK, const uint32_t* NK,
                         uint32_t n, uint32_t passes, uint32_t* a_key, uint32_t* a_val, uint32_t* b_key,
                         uint32_t* b_val, uint32_t* hist, unsigned long long* lookback, uint32_t* ticket,
-                        uint32_t* counts, uint32_t* err);
+                        uint32_t* counts, uint32_t* err, unsigned long long* changed_total = nullptr);
 cudaError_t launch_merge(cudaStream_t s, const uint32_t* a_key, const uint32_t* a_val, const uint32_t* b_key,
                          const uint32_t* b_val, const uint32_t* counts, uint32_t* split, uint32_t n,
                          uint32_t* out_key, uint32_t* out_val, const float2* pos, float2* sorted_pos,
@@ -86,6 +87,9 @@ cudaError_t launch_iota(cudaStream_t s, uint32_t* out, uint32_t n);
 // *first_bad = first i with (head[i] & road mask) >= num_roads, or 0xffffffff
 cudaError_t launch_check_roads(cudaStream_t s, const uint32_t* head, uint32_t n, uint32_t num_roads,
                                uint32_t* first_bad);
+// The same over entities [first, first + n) without resetting *first_bad (atomic min).
+cudaError_t launch_check_roads_range(cudaStream_t s, const uint32_t* head, uint32_t first, uint32_t n,
+                                     uint32_t num_roads, uint32_t* first_bad);
 cudaError_t launch_fill(cudaStream_t s, float* out, uint32_t n, float v);
 cudaError_t launch_permute(cudaStream_t s, const uint32_t* sorted_slot, EntityState src,
                            EntityState dst, uint32_t n);

@@ -1,0 +1,112 @@
+"""msim_tick_host: one tick with the entity state on the host (chunked upload, move,
+download, then index + query), against the same tick through the separate calls
+(msim_set_entities, msim_step, msim_get_state, msim_get_neighbours) and the oracle.
+Everything is compared bit for bit."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _same_state(a, b, what):
+    assert np.array_equal(a["pos"].view(np.uint32), b["pos"].view(np.uint32)), f"positions differ {what}"
+    assert np.array_equal(a["heading"], b["heading"]), f"headings differ {what}"
+    assert np.array_equal(a["rng"], b["rng"]), f"RNG states differ {what}"
+
+
+@pytest.mark.parametrize("n", [300_000, 70_000, 1])
+def test_tick_host_matches_separate_calls_and_oracle(msim, orc, n):
+    """300,000 entities go in five chunks of 65,536 (the last ragged), 70,000 in two."""
+    road_map = msim.RoadMap.lattice(64, 9)
+    kw = dict(rng="pcg32", dt=0.1, radius=2.0, cap=16)
+    with msim.Simulation(road_map, n, **kw) as a, msim.Simulation(road_map, n, **kw) as b:
+        a.init_entities(5, placement="fraction", speed=(1.0, 1.6))
+        st = a.get_state()
+        speed = st["speed"].copy()
+        pos, head, rng = st["pos"].copy(), st["heading"].copy(), st["rng"].copy()
+        out = {"pos": msim.PinnedBuffer((n, 2), np.float32), "heading": msim.PinnedBuffer(n, np.uint32),
+               "rng": msim.PinnedBuffer((n, 4), np.uint32), "count": msim.PinnedBuffer(n, np.uint32),
+               "idx": msim.PinnedBuffer((n, 16), np.uint32)}
+        arrays = {k: v.array for k, v in out.items()}
+        for t in range(3):
+            got = a.tick_host(st, neighbours=True, out=arrays)
+            b.set_entities(st["pos"], st["heading"], st["rng"], st["speed"])
+            b.step(1, neighbours=True)
+            ref = b.get_state()
+            cnt, idx = b.get_neighbours()
+            _same_state(got, ref, f"from the separate calls at tick {t + 1}")
+            assert np.array_equal(got["count"], cnt) and np.array_equal(got["idx"], idx)
+            orc.step(road_map.road_pos, road_map.road_conn, road_map.connections, pos, head, rng, speed, 1, 0.1, 1,
+                     threads=8)
+            ocnt, oidx, _ = orc.neighbours(pos, 2.0, 16, threads=8)
+            _same_state(got, {"pos": pos, "heading": head, "rng": rng}, f"from the oracle at tick {t + 1}")
+            assert np.array_equal(got["count"], ocnt) and np.array_equal(got["idx"], oidx)
+            st = {"pos": got["pos"].copy(), "heading": got["heading"].copy(), "rng": got["rng"].copy(),
+                  "speed": speed}
+        assert a.tick == 3
+        assert a.collision_pairs() == int(ocnt.sum()) // 2
+        for buf in out.values():
+            buf.free()
+
+
+@pytest.mark.parametrize("index", ["incremental", "full"])
+def test_ticks_after_tick_host(msim, orc, index):
+    """Regular neighbour ticks after a host tick (re-ordering on the next tick, then
+    incremental or full index updates) stay equal to the oracle."""
+    road_map = msim.RoadMap.lattice(40, 3)
+    n = 90_000
+    with msim.Simulation(road_map, n, rng="xorshift128", dt=0.1, radius=2.0, cap=8, resort_interval=4,
+                         index=index) as sim:
+        sim.init_entities(8, placement="fraction", speed=(1.0, 1.6))
+        st = sim.get_state()
+        pos, head, rng, speed = st["pos"].copy(), st["heading"].copy(), st["rng"].copy(), st["speed"].copy()
+        sim.tick_host(st, neighbours=True)
+        orc.step(road_map.road_pos, road_map.road_conn, road_map.connections, pos, head, rng, speed, 0, 0.1, 1)
+        for t in range(10):
+            sim.step(1, neighbours=True)
+            orc.step(road_map.road_pos, road_map.road_conn, road_map.connections, pos, head, rng, speed, 0, 0.1, 1)
+            _same_state(sim.get_state(), {"pos": pos, "heading": head, "rng": rng}, f"at tick {t + 2}")
+            cnt, idx = sim.get_neighbours()
+            ocnt, oidx, _ = orc.neighbours(pos, 2.0, 8, threads=8)
+            assert np.array_equal(cnt, ocnt) and np.array_equal(idx, oidx), f"neighbours differ at tick {t + 2}"
+
+
+def test_tick_host_move_only_default_speed(msim, orc):
+    """Without MSIM_STEP_NEIGHBOURS and without speeds: SPEED = 1.4 m per tick at dt = 1
+    (reference mode), no neighbour outputs."""
+    road_map = msim.RoadMap.lattice(16, 2)
+    n = 20_000
+    with msim.Simulation(road_map, n, rng="xorshift128", dt=1.0, radius=10.0, cap=4) as sim:
+        sim.init_entities(3, placement="start", speed=(1.4, 1.4))
+        st = sim.get_state()
+        pos, head, rng = st["pos"].copy(), st["heading"].copy(), st["rng"].copy()
+        speed = np.full(n, 1.4, np.float32)
+        state = {"pos": st["pos"], "heading": st["heading"], "rng": st["rng"]}
+        for t in range(5):
+            state = sim.tick_host(state, neighbours=False)
+            assert "count" not in state
+            orc.step(road_map.road_pos, road_map.road_conn, road_map.connections, pos, head, rng, speed, 0, 1.0, 1)
+            _same_state(state, {"pos": pos, "heading": head, "rng": rng}, f"at tick {t + 1}")
+        with pytest.raises(msim.MsimError) as e:  # no neighbour tick has run
+            sim.get_neighbours()
+        assert e.value.code == 1
+
+
+def test_tick_host_bad_heading_keeps_state(msim):
+    road_map = msim.RoadMap.lattice(16, 2)
+    n = 100_000
+    with msim.Simulation(road_map, n, rng="pcg32", dt=0.1, radius=2.0, cap=4) as sim:
+        sim.init_entities(1, placement="fraction", speed=(1.0, 1.6))
+        sim.step(2, neighbours=True)
+        before = sim.get_state()
+        bad = {k: v.copy() for k, v in before.items()}
+        bad["heading"][77_777] = road_map.num_roads  # in the second chunk
+        with pytest.raises(msim.MsimError) as e:
+            sim.tick_host(bad, neighbours=True)
+        assert e.value.code == 2 and "77777" in str(e.value)
+        after = sim.get_state()
+        for k in before:
+            assert np.array_equal(before[k], after[k])
+        assert sim.tick == 2
+        sim.step(1, neighbours=True)  # the context stays usable
+        sim.sync()
