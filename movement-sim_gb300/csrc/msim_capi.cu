@@ -82,6 +82,7 @@ struct msim_ctx {
     // incremental index update: the previous order split into unchanged (a) and
     // changed (b, sorted in place with ping-pong) keys, then merged
     bool order_identity = false;  // sorted_slot[q] == q (right after a re-ordering)
+    bool slots_identity = false;  // slot s holds entity s (state set from the host, not re-ordered since)
     bool incremental = true;      // index updates from the previous order (else full sorts)
     uint32_t* a_key = nullptr;
     uint32_t* a_val = nullptr;
@@ -340,6 +341,7 @@ int permute_state(msim_ctx* c) {
     c->cur = 1 - c->cur;
     c->have_sort = false;
     c->order_identity = true;  // slot q now holds the entity at sorted position q
+    c->slots_identity = false;
     c->since_permute = 0;
     return MSIM_OK;
 }
@@ -368,14 +370,21 @@ int build_index(msim_ctx* c) {
 // One tick of the move plus the index, from the previous sorted order: split it by
 // whether each key changed, sort the changed entries, merge (writing the key-start
 // table and the sorted positions on the way).
+int incremental_update(msim_ctx* c);
+
 int incremental_index(msim_ctx* c) {
-    CK(cudaMemsetAsync(c->hist, 0, sizeof(uint32_t) * kMaxPasses * kRadix, c->stream), "memset hist");
     {
         Prof p(c, K_STEP);
         StepLaunch a = step_args(c, 1, true);
         a.hist = nullptr;  // the changed keys' digits are counted by k_mark
         CK(launch_step(c->stream, a), "k_step");
     }
+    return incremental_update(c);
+}
+
+// The update itself, for new keys (by slot) already in c->key.
+int incremental_update(msim_ctx* c) {
+    CK(cudaMemsetAsync(c->hist, 0, sizeof(uint32_t) * kMaxPasses * kRadix, c->stream), "memset hist");
     {
         Prof p(c, K_MARK);
         CK(launch_mark(c->stream, c->sorted_slot, c->order_identity, c->sorted_key, c->key, c->n, c->passes,
@@ -717,6 +726,7 @@ int msim_set_entities(msim_ctx* c, const float* pos, const uint32_t* heading, co
     // pays it).
     CK(launch_iota(c->stream, s.slot_id, c->n), "k_iota");
     reset_index(c);
+    c->slots_identity = true;
     return MSIM_OK;
 }
 
@@ -848,8 +858,13 @@ int msim_tick_host(msim_ctx* c, const float* in_pos, const uint32_t* in_heading,
     const int old = c->cur;
     const int b = 1 - old;
     EntityState& s = c->st[b];
+    // The previous index stays a valid starting order for an incremental update when
+    // its slots already held entity ids (the previous call was a host tick, or a set
+    // followed by one tick): the new state goes to the same slots.
+    const bool old_slots_identity = c->slots_identity;
+    const bool use_inc = nbr && c->incremental && c->sorted_key && c->slots_identity;
     CK(cudaMemsetAsync(c->check, 0xff, sizeof(uint32_t), c->stream), "memset check");
-    if (nbr) CK(cudaMemsetAsync(c->hist, 0, sizeof(uint32_t) * kMaxPasses * kRadix, c->stream), "memset hist");
+    if (nbr && !use_inc) CK(cudaMemsetAsync(c->hist, 0, sizeof(uint32_t) * kMaxPasses * kRadix, c->stream), "memset hist");
     CK(cudaEventRecord(c->ev_start, c->stream), "cudaEventRecord");
     CK(cudaStreamWaitEvent(c->up, c->ev_start, 0), "cudaStreamWaitEvent");
 
@@ -882,6 +897,7 @@ int msim_tick_host(msim_ctx* c, const float* in_pos, const uint32_t* in_heading,
             a.st.slot_id = s.slot_id + lo;
             a.n = cnt;
             a.key = nbr ? c->key + lo : nullptr;
+            if (use_inc) a.hist = nullptr;  // the changed keys' digits are counted by k_mark
             a.blocks = std::min<int>(c->step_blocks, (int)((cnt + kStepThreads - 1) / kStepThreads));
             CK(launch_step(c->stream, a), "k_step");
         }
@@ -901,11 +917,15 @@ int msim_tick_host(msim_ctx* c, const float* in_pos, const uint32_t* in_heading,
     }
     CK(launch_iota(c->stream, s.slot_id, n), "k_iota");  // entity i in slot i
     c->cur = b;
-    reset_index(c);
+    c->slots_identity = true;
+    if (use_inc) {
+        if ((rc = incremental_update(c)) != MSIM_OK) return rc;
+    } else {
+        reset_index(c);
+        if (nbr && ((rc = sort_keys(c)) != MSIM_OK || (rc = key_start_table(c)) != MSIM_OK)) return rc;
+    }
     if (nbr) {
-        if ((rc = sort_keys(c)) != MSIM_OK || (rc = key_start_table(c)) != MSIM_OK ||
-            (rc = run_query(c, false)) != MSIM_OK)
-            return rc;
+        if ((rc = run_query(c, false)) != MSIM_OK) return rc;
         if (out_count || out_idx) {
             const bool want_idx = out_idx && c->params.cap;
             const size_t cap = c->params.cap;
@@ -935,6 +955,7 @@ int msim_tick_host(msim_ctx* c, const float* in_pos, const uint32_t* in_heading,
     if (first_bad != 0xffffffffu) {  // as msim_set_entities: the previous state stays
         c->cur = old;
         reset_index(c);
+        c->slots_identity = old_slots_identity;
         c->tick--;
         CK(cudaMemsetAsync(c->err, 0, sizeof(uint32_t), c->stream), "clear device status");
         CK(cudaStreamSynchronize(c->stream), "cudaStreamSynchronize");

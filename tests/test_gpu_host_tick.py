@@ -14,12 +14,14 @@ def _same_state(a, b, what):
     assert np.array_equal(a["rng"], b["rng"]), f"RNG states differ {what}"
 
 
-@pytest.mark.parametrize("n", [300_000, 70_000, 1])
-def test_tick_host_matches_separate_calls_and_oracle(msim, orc, n):
-    """300,000 entities go in five chunks of 65,536 (the last ragged), 70,000 in two."""
+@pytest.mark.parametrize("n,index", [(300_000, "auto"), (300_000, "incremental"), (70_000, "incremental"),
+                                     (1, "auto")])
+def test_tick_host_matches_separate_calls_and_oracle(msim, orc, n, index):
+    """300,000 entities go in five chunks of 65,536 (the last ragged), 70,000 in two.
+    With the incremental index, host ticks after the first update the previous order."""
     road_map = msim.RoadMap.lattice(64, 9)
     kw = dict(rng="pcg32", dt=0.1, radius=2.0, cap=16)
-    with msim.Simulation(road_map, n, **kw) as a, msim.Simulation(road_map, n, **kw) as b:
+    with msim.Simulation(road_map, n, index=index, **kw) as a, msim.Simulation(road_map, n, **kw) as b:
         a.init_entities(5, placement="fraction", speed=(1.0, 1.6))
         st = a.get_state()
         speed = st["speed"].copy()
@@ -28,7 +30,7 @@ def test_tick_host_matches_separate_calls_and_oracle(msim, orc, n):
                "rng": msim.PinnedBuffer((n, 4), np.uint32), "count": msim.PinnedBuffer(n, np.uint32),
                "idx": msim.PinnedBuffer((n, 16), np.uint32)}
         arrays = {k: v.array for k, v in out.items()}
-        for t in range(3):
+        for t in range(4):
             got = a.tick_host(st, neighbours=True, out=arrays)
             b.set_entities(st["pos"], st["heading"], st["rng"], st["speed"])
             b.step(1, neighbours=True)
@@ -43,7 +45,7 @@ def test_tick_host_matches_separate_calls_and_oracle(msim, orc, n):
             assert np.array_equal(got["count"], ocnt) and np.array_equal(got["idx"], oidx)
             st = {"pos": got["pos"].copy(), "heading": got["heading"].copy(), "rng": got["rng"].copy(),
                   "speed": speed}
-        assert a.tick == 3
+        assert a.tick == 4
         assert a.collision_pairs() == int(ocnt.sum()) // 2
         for buf in out.values():
             buf.free()
@@ -110,3 +112,40 @@ def test_tick_host_bad_heading_keeps_state(msim):
         assert sim.tick == 2
         sim.step(1, neighbours=True)  # the context stays usable
         sim.sync()
+
+
+def test_host_ticks_with_host_edits_and_mixed_calls(msim, orc):
+    """Incremental host ticks while the host moves entities between ticks (teleports
+    to other roads: many keys change at once), then regular ticks (the second
+    re-orders the state), then a host tick again (a full sort, as the slots no longer
+    hold entity ids)."""
+    road_map = msim.RoadMap.lattice(48, 4)
+    n = 150_000
+    rs = np.random.default_rng(0)
+    with msim.Simulation(road_map, n, rng="pcg32", dt=0.1, radius=2.0, cap=8, index="incremental") as sim:
+        sim.init_entities(2, placement="fraction", speed=(1.0, 1.6))
+        st = sim.get_state()
+        speed = st["speed"].copy()
+        state = {"pos": st["pos"].copy(), "heading": st["heading"].copy(), "rng": st["rng"].copy(), "speed": speed}
+        for t in range(6):
+            if t in (2, 5):  # the host teleports 20,000 entities to the start of random roads
+                who = rs.choice(n, 20_000, replace=False)
+                roads = rs.integers(0, road_map.num_roads, who.size)
+                state["pos"][who] = road_map.road_pos[roads, :2]
+                state["heading"][who] = roads.astype(np.uint32) | np.uint32(0x80000000)
+            pos, head, rng = state["pos"].copy(), state["heading"].copy(), state["rng"].copy()
+            if t in (3, 4):  # regular ticks in between (the second re-orders the state)
+                if t == 3:
+                    sim.set_entities(state["pos"], state["heading"], state["rng"], speed)
+                sim.step(1, neighbours=True)
+                got = sim.get_state()
+                got["count"] = sim.get_neighbours(with_idx=False)[0]
+            else:
+                got = sim.tick_host(state, neighbours=True)
+            orc.step(road_map.road_pos, road_map.road_conn, road_map.connections, pos, head, rng, speed, 1, 0.1, 1,
+                     threads=8)
+            _same_state(got, {"pos": pos, "heading": head, "rng": rng}, f"at tick {t + 1}")
+            ocnt, _, _ = orc.neighbours(pos, 2.0, 8, threads=8, with_idx=False)
+            assert np.array_equal(got["count"], ocnt), f"counts differ at tick {t + 1}"
+            state = {"pos": got["pos"].copy(), "heading": got["heading"].copy(), "rng": got["rng"].copy(),
+                     "speed": speed}
