@@ -71,10 +71,11 @@ KERNEL_BYTES = {
 }
 
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per entity and launch of
-# one ncu capture per workload (profiles/*_ncu.md); scaled by the entities of the run
+# one ncu capture of the same workload at full size (third neighbour tick; 1-pass
+# metrics; profiles/scale_16M_dram_traffic.md); scaled by the entities of the run
 NCU_DRAM_BYTES_PER_ENTITY = {
-    "scale": {},
-    "neighbours": {},
+    "scale": {"k_query": 26.83, "k_merge": 32.49, "k_mark": 17.06, "k_step": 28.18},
+    "neighbours": {"k_query": 24.10},
 }
 
 

@@ -70,10 +70,18 @@ struct msim_ctx {
     uint32_t* digit_off = nullptr;
     uint32_t* lookback = nullptr;
     uint32_t* tickets = nullptr;
+    // The index the query reads (current buffer set).  Two sets, paired with the two
+    // sorted-slot buffers: a tick's merge writes the set the previous tick's query does
+    // not read, so that query overlaps the next tick up to its merge.
     uint32_t* kstart = nullptr;  // first sorted position of every key, 2^key_bits + 1 entries
     uint4* kstart_chunks = nullptr;  // long key gaps, filled by a second kernel
     float2* sorted_pos = nullptr;    // positions in sorted order (the query's candidates)
     uint32_t* kstart_chunk_count = nullptr;
+    uint32_t* kstart_b[2] = {nullptr, nullptr};
+    uint4* kstart_chunks_b[2] = {nullptr, nullptr};
+    float2* sorted_pos_b[2] = {nullptr, nullptr};
+    uint32_t* kstart_chunk_count_b[2] = {nullptr, nullptr};
+    int ib = 0;  // current index buffer set
     size_t num_keys = 0;
     uint32_t sort_tiles = 0;
     const uint32_t* sorted_key = nullptr;
@@ -130,8 +138,8 @@ struct msim_ctx {
     // the query of tick t runs on qstream while the main stream moves tick t + 1
     cudaStream_t qstream = nullptr;
     cudaEvent_t ev_index = nullptr;  // key-start table and sorted positions of tick t ready
-    cudaEvent_t ev_query = nullptr;  // query of tick t done
-    bool query_pending = false;
+    cudaEvent_t ev_read[2] = {nullptr, nullptr};  // the last query on index buffer set b is done
+    bool read_pending[2] = {false, false};
     // host round trip (msim_tick_host): upload and download streams, per-chunk events
     cudaStream_t up = nullptr, down = nullptr;
     cudaEvent_t ev_start = nullptr;
@@ -194,7 +202,8 @@ void free_all(msim_ctx* c) {
     if (c->t0) cudaEventDestroy(c->t0);
     if (c->t1) cudaEventDestroy(c->t1);
     if (c->ev_index) cudaEventDestroy(c->ev_index);
-    if (c->ev_query) cudaEventDestroy(c->ev_query);
+    for (int b = 0; b < 2; b++)
+        if (c->ev_read[b]) cudaEventDestroy(c->ev_read[b]);
     if (c->qstream) cudaStreamDestroy(c->qstream);
     if (c->ev_start) cudaEventDestroy(c->ev_start);
     for (uint32_t k = 0; k < kHostChunks; k++) {
@@ -287,12 +296,27 @@ StepLaunch step_args(msim_ctx* c, uint32_t ticks, bool key) {
     return a;
 }
 
-// The main stream waits for a query still running on qstream.
-int join_query(msim_ctx* c) {
-    if (!c->query_pending) return MSIM_OK;
-    CK(cudaStreamWaitEvent(c->stream, c->ev_query, 0), "cudaStreamWaitEvent");
-    c->query_pending = false;
+// The main stream waits for the queries still running on qstream that read index
+// buffer set b (wait_reads) or any set (join_query).
+int wait_reads(msim_ctx* c, int b) {
+    if (!c->read_pending[b]) return MSIM_OK;
+    CK(cudaStreamWaitEvent(c->stream, c->ev_read[b], 0), "cudaStreamWaitEvent");
+    c->read_pending[b] = false;
     return MSIM_OK;
+}
+
+int join_query(msim_ctx* c) {
+    int rc = wait_reads(c, 0);
+    return rc != MSIM_OK ? rc : wait_reads(c, 1);
+}
+
+// The next index is written to buffer set b (the set paired with its sorted slots).
+void use_index_buffers(msim_ctx* c, int b) {
+    c->ib = b;
+    c->kstart = c->kstart_b[b];
+    c->kstart_chunks = c->kstart_chunks_b[b];
+    c->sorted_pos = c->sorted_pos_b[b];
+    c->kstart_chunk_count = c->kstart_chunk_count_b[b];
 }
 
 int sort_keys(msim_ctx* c);
@@ -336,6 +360,9 @@ int sort_keys(msim_ctx* c) {
 }
 
 int permute_state(msim_ctx* c) {
+    // the target state buffer holds the slot ids a query two ticks back may still read
+    int rc = join_query(c);
+    if (rc != MSIM_OK) return rc;
     Prof p(c, K_PERMUTE);
     CK(launch_permute(c->stream, c->sorted_slot, c->st[c->cur], c->st[1 - c->cur], c->n), "k_permute");
     c->cur = 1 - c->cur;
@@ -408,9 +435,12 @@ int incremental_update(msim_ctx* c) {
                            c->ab_counts + 1),
            "k_onesweep");
     }
-    int rc = join_query(c);  // the merge rewrites the table and sorted positions the last query reads
-    if (rc != MSIM_OK) return rc;
+    // The merge writes the sorted slots and index buffer set the previous tick's query
+    // does not read (that query may still run); it waits for the query before that.
     const int out = c->sorted_key == c->sk[0] ? 1 : 0;
+    int rc = wait_reads(c, out);
+    if (rc != MSIM_OK) return rc;
+    use_index_buffers(c, out);
     {
         Prof p(c, K_MERGE);
         uint32_t launched = 0;
@@ -452,6 +482,8 @@ int neighbour_tick(msim_ctx* c) {
 // key-start table and positions in sorted order, after a full sort
 int key_start_table(msim_ctx* c) {
     c->order_identity = false;
+    // after a full sort (every query joined): the set paired with the final slot buffer
+    use_index_buffers(c, c->sorted_slot == c->sv[0] ? 0 : 1);
     Prof p(c, K_KSTART);
     uint32_t launched = 0;
     CK(launch_kstart(c->stream, c->sorted_key, c->n, c->kstart, (uint32_t)c->num_keys, c->kstart_chunks,
@@ -480,8 +512,8 @@ int run_query(msim_ctx* c, bool overlap) {
            "k_query");
     }
     if (qs != c->stream) {
-        CK(cudaEventRecord(c->ev_query, qs), "cudaEventRecord");
-        c->query_pending = true;
+        CK(cudaEventRecord(c->ev_read[c->ib], qs), "cudaEventRecord");
+        c->read_pending[c->ib] = true;
     }
     c->have_nbr = true;
     c->since_permute++;
@@ -562,7 +594,8 @@ int msim_create(const msim_map* map, const msim_params* params, msim_ctx** out) 
     if (e != cudaSuccess) return bail(cuda_fail(e, "cudaStreamCreate"));
     if (cudaEventCreate(&c->t0) != cudaSuccess || cudaEventCreate(&c->t1) != cudaSuccess ||
         cudaEventCreateWithFlags(&c->ev_index, cudaEventDisableTiming) != cudaSuccess ||
-        cudaEventCreateWithFlags(&c->ev_query, cudaEventDisableTiming) != cudaSuccess)
+        cudaEventCreateWithFlags(&c->ev_read[0], cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c->ev_read[1], cudaEventDisableTiming) != cudaSuccess)
         return bail(fail(MSIM_ERR_CUDA, "cudaEventCreate failed"));
 
     // ---- spatial grid ----
@@ -627,9 +660,7 @@ int msim_create(const msim_map* map, const msim_params* params, msim_ctx** out) 
     if ((rc = dalloc(c, &c->key, n)) || (rc = dalloc(c, &c->hist, (size_t)kMaxPasses * kRadix)) ||
         (rc = dalloc(c, &c->digit_off, (size_t)kMaxPasses * kRadix)) ||
         (rc = dalloc(c, &c->lookback, (size_t)kMaxPasses * c->sort_tiles * kRadix)) ||
-        (rc = dalloc(c, &c->tickets, (size_t)kMaxPasses)) || (rc = dalloc(c, &c->kstart, c->num_keys + 1)) ||
-        (rc = dalloc(c, &c->kstart_chunks, kstart_chunks(c->num_keys))) || (rc = dalloc(c, &c->kstart_chunk_count, 1)) ||
-        (rc = dalloc(c, &c->sorted_pos, n)) || (rc = dalloc(c, &c->a_key, n)) || (rc = dalloc(c, &c->a_val, n)) ||
+        (rc = dalloc(c, &c->tickets, (size_t)kMaxPasses)) || (rc = dalloc(c, &c->a_key, n)) || (rc = dalloc(c, &c->a_val, n)) ||
         (rc = dalloc(c, &c->b_key[0], n)) || (rc = dalloc(c, &c->b_key[1], n)) || (rc = dalloc(c, &c->b_val[0], n)) ||
         (rc = dalloc(c, &c->b_val[1], n)) || (rc = dalloc(c, &c->ab_counts, 2)) ||
         (rc = dalloc(c, &c->mark_lookback, mark_tiles(c->n))) || (rc = dalloc(c, &c->mark_ticket, 1)) ||
@@ -637,6 +668,13 @@ int msim_create(const msim_map* map, const msim_params* params, msim_ctx** out) 
         (rc = dalloc(c, &c->nbr_count, n)) || (rc = dalloc(c, &c->pairs, kPairBins)) || (rc = dalloc(c, &c->err, 1)) ||
         (rc = dalloc(c, &c->check, 1)))
         return bail(rc);
+    for (int b = 0; b < 2; b++) {
+        if ((rc = dalloc(c, &c->kstart_b[b], c->num_keys + 1)) ||
+            (rc = dalloc(c, &c->kstart_chunks_b[b], kstart_chunks(c->num_keys))) ||
+            (rc = dalloc(c, &c->kstart_chunk_count_b[b], 1)) || (rc = dalloc(c, &c->sorted_pos_b[b], n)))
+            return bail(rc);
+    }
+    use_index_buffers(c, 0);
     if (p.cap > 0) {
         size_t blocks = (n + kQueryThreads - 1) / kQueryThreads;
         if ((rc = dalloc(c, &c->nbr_list, blocks * kQueryThreads * (size_t)p.cap))) return bail(rc);

@@ -420,20 +420,9 @@ __global__ void k_ranges(const uint32_t* __restrict__ sk, uint32_t n, uint32_t* 
     }
 }
 
-// The ascending list of the kRegKeep smallest ids, kept in registers.
+// The query keeps the sorted positions of an entity's first kRegKeep neighbours in
+// shared memory; entities with more take list_overflow.
 constexpr int kRegKeep = 4;
-__device__ __forceinline__ void keep_smallest(uint32_t (&r)[kRegKeep], uint32_t id) {
-    if (id >= r[kRegKeep - 1]) return;
-    r[kRegKeep - 1] = id;
-#pragma unroll
-    for (int i = kRegKeep - 1; i > 0; i--) {
-        if (r[i] < r[i - 1]) {
-            const uint32_t t = r[i];
-            r[i] = r[i - 1];
-            r[i - 1] = t;
-        }
-    }
-}
 
 // Exact ascending list of the cap smallest ids of one entity, written by
 // insertion straight into its output slots; for the rare entities with more
