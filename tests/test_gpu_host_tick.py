@@ -38,6 +38,10 @@ def test_tick_host_matches_separate_calls_and_oracle(msim, orc, n, index):
             cnt, idx = b.get_neighbours()
             _same_state(got, ref, f"from the separate calls at tick {t + 1}")
             assert np.array_equal(got["count"], cnt) and np.array_equal(got["idx"], idx)
+            # the context's own exports agree (its state may now sit in another slot order)
+            _same_state(a.get_state(), ref, f"from the context after the host tick {t + 1}")
+            acnt, aidx = a.get_neighbours()
+            assert np.array_equal(acnt, cnt) and np.array_equal(aidx, idx)
             orc.step(road_map.road_pos, road_map.road_conn, road_map.connections, pos, head, rng, speed, 1, 0.1, 1,
                      threads=8)
             ocnt, oidx, _ = orc.neighbours(pos, 2.0, 16, threads=8)
