@@ -15,7 +15,8 @@ constexpr uint32_t kMarkThreads = 256;
 constexpr uint32_t kMarkPer = 16;                           // rows of a tile (entries per thread)
 constexpr uint32_t kMarkTile = kMarkThreads * kMarkPer;     // 4096
 constexpr uint32_t kMergeThreads = 256;
-constexpr uint32_t kMergeTile = 2048;                       // output positions per block
+constexpr uint32_t kMergeTile = 1024;                       // output positions per block (16 M:
+                                                            // 0.177 ms per merge, 0.190 with 2048)
 // look-back word of k_mark: flag (bits 62-63) | A count (bits 31-61) | B count (bits 0-30)
 constexpr unsigned long long kMarkAgg = 1ull << 62;
 constexpr unsigned long long kMarkPrefix = 2ull << 62;
@@ -37,8 +38,10 @@ __device__ __forceinline__ void st_relaxed64(unsigned long long* p, unsigned lon
 // A and B entries are staged in q order in shared memory and written out coalesced.
 // Tiles are taken in ticket order and find their output offsets by a warp-wide
 // decoupled look-back (32 predecessors per round of loads).  identity: P[q] = q
-// (right after the state was re-ordered).
-__global__ __launch_bounds__(kMarkThreads) void k_mark(const uint32_t* __restrict__ P, uint32_t identity,
+// (right after the state was re-ordered).  Five blocks per SM (48 registers): the
+// split waits on its barriers and look-back, so more resident tiles hide that
+// (measured at 16 M: 0.114 ms against 0.120 with four blocks, 0.118 with six).
+__global__ __launch_bounds__(kMarkThreads, 5) void k_mark(const uint32_t* __restrict__ P, uint32_t identity,
                                                        const uint32_t* __restrict__ PK,
                                                        const uint32_t* __restrict__ NK, uint32_t n, uint32_t passes,
                                                        uint32_t* __restrict__ a_key, uint32_t* __restrict__ a_val,
@@ -51,6 +54,7 @@ __global__ __launch_bounds__(kMarkThreads) void k_mark(const uint32_t* __restric
     __shared__ uint32_t s_key[kMarkTile], s_val[kMarkTile];  // A entries, then B entries, in q order
     __shared__ uint32_t s_hist[kMaxPasses * kRadix];
     __shared__ uint32_t s_off[kMarkPer * NW + 1];            // exclusive A counts before (row, warp)
+    __shared__ uint32_t s_bal[kMarkPer * NW];                // the (row, warp) ballots of unchanged keys
     __shared__ uint32_t s_tile, s_pa, s_pb;
     const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     if (tid == 0) s_tile = atomicAdd(ticket, 1u);
@@ -59,8 +63,9 @@ __global__ __launch_bounds__(kMarkThreads) void k_mark(const uint32_t* __restric
     const uint32_t tile = s_tile;
     const uint32_t base = tile * kMarkTile;
     const uint32_t lt = lanemask_lt();
-    uint32_t kn[kMarkPer], sl[kMarkPer], rank[kMarkPer];
-    uint32_t unch = 0u;
+    // the row ballots go to shared memory (each lane's rank and A/B side come back from
+    // them at staging), so a thread holds only its keys and slots: fewer registers
+    uint32_t kn[kMarkPer], sl[kMarkPer];
 #pragma unroll
     for (uint32_t r = 0; r < kMarkPer; r++) {
         const uint32_t q = base + r * kMarkThreads + tid;
@@ -73,9 +78,10 @@ __global__ __launch_bounds__(kMarkThreads) void k_mark(const uint32_t* __restric
             u = kn[r] == PK[q];
         }
         const unsigned bal = __ballot_sync(FULL, u);
-        rank[r] = (uint32_t)__popc(bal & lt);  // A rank inside this row and warp (for now)
-        if (u) unch |= 1u << r;
-        if (lane == 0) s_off[r * NW + warp] = (uint32_t)__popc(bal);
+        if (lane == 0) {
+            s_off[r * NW + warp] = (uint32_t)__popc(bal);
+            s_bal[r * NW + warp] = bal;
+        }
     }
     __syncthreads();
     if (warp == 0) {  // exclusive scan of the kMarkPer * NW counts, in (row, warp) order
@@ -108,13 +114,15 @@ __global__ __launch_bounds__(kMarkThreads) void k_mark(const uint32_t* __restric
     for (uint32_t r = 0; r < kMarkPer; r++) {  // stage in shared memory: A at [0, tot_a), B after
         const uint32_t i = r * kMarkThreads + tid;  // linear index in the tile = q - base
         if (i >= valid_in_tile) continue;
-        const uint32_t ra = s_off[r * NW + warp] + rank[r];
-        const uint32_t dst = ((unch >> r) & 1u) ? ra : tot_a + (i - ra);
+        const unsigned bal = s_bal[r * NW + warp];
+        const bool u = (bal >> lane) & 1u;
+        const uint32_t ra = s_off[r * NW + warp] + (uint32_t)__popc(bal & lt);  // A entries before it
+        const uint32_t dst = u ? ra : tot_a + (i - ra);
         if (dst < kMarkTile) {
             s_key[dst] = kn[r];
             s_val[dst] = sl[r];
         }
-        if (!((unch >> r) & 1u))
+        if (!u)
             for (uint32_t ps = 0; ps < passes; ps++)
                 atomicAdd(&s_hist[ps * kRadix + ((kn[r] >> (8u * ps)) & 0xffu)], 1u);
     }
@@ -180,22 +188,41 @@ __global__ __launch_bounds__(kMarkThreads) void k_mark(const uint32_t* __restric
 }
 
 // Merge path: split[t] = number of A entries among the first min(t * kMergeTile, n)
-// entries of the merge (A first on equal keys).  One thread per tile boundary.
+// entries of the merge (A first on equal keys): the first i in [max(0, d - |B|),
+// min(d, |A|)] with A[i] > B[d - 1 - i] (or the upper end).  One warp per tile
+// boundary, 32-ary search: 32 probes per round, so about five rounds of dependent
+// loads at 16 M entries instead of 24 for a binary search.
 __global__ __launch_bounds__(256) void k_merge_path(const uint32_t* __restrict__ a_key,
                                                     const uint32_t* __restrict__ b_key,
                                                     const uint32_t* __restrict__ counts, uint32_t n,
                                                     uint32_t boundaries, uint32_t* __restrict__ split) {
-    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= boundaries) return;
+    constexpr uint32_t FULL = 0xffffffffu;
+    const uint32_t t = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint32_t lane = threadIdx.x & 31;
+    if (t >= boundaries) return;  // uniform per warp
     const uint32_t na = counts[0], nb = counts[1];
     const uint32_t d = min(t * kMergeTile, n);
+    // the answer stays in [lo, hi]; A[hi] > B[d - 1 - hi] or hi is the upper end
     uint32_t lo = d > nb ? d - nb : 0u, hi = min(d, na);
-    while (lo < hi) {
-        const uint32_t mid = lo + ((hi - lo) >> 1);
-        if (a_key[mid] <= b_key[d - mid - 1u]) lo = mid + 1u;
-        else hi = mid;
+    while (hi - lo > 32u) {
+        const uint32_t step = (hi - lo + 31u) >> 5;
+        const uint32_t i = min(lo + (lane + 1u) * step - 1u, hi - 1u);
+        const unsigned m = __ballot_sync(FULL, a_key[i] > b_key[d - 1u - i]);
+        if (m == 0u) {  // the last probe is hi - 1: every index below hi belongs to the prefix
+            lo = hi;
+            break;
+        }
+        const uint32_t f = __ffs(m) - 1u;
+        const uint32_t xf = min(lo + (f + 1u) * step - 1u, hi - 1u);
+        lo = f ? min(lo + f * step - 1u, hi - 1u) + 1u : lo;
+        hi = xf;
     }
-    split[t] = lo;
+    if (hi > lo) {
+        const uint32_t i = lo + lane;
+        const unsigned m = __ballot_sync(FULL, i < hi && a_key[i] > b_key[d - 1u - i]);
+        lo = m ? lo + __ffs(m) - 1u : hi;
+    }
+    if (lane == 0) split[t] = lo;
 }
 
 // Merges tile t of the output: A entries [split[t], split[t+1]) and the matching B

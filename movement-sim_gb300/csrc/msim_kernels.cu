@@ -25,6 +25,7 @@ constexpr uint32_t kFlagPrefix = 0x80000000u;
 constexpr uint32_t kFlagMask = 0xc0000000u;
 constexpr uint32_t kValueMask = 0x3fffffffu;
 constexpr uint32_t kSpinLimit = 1u << 24;  // ~1 s of polling, then give up with kErrTimeout
+constexpr int kLookBack = 4;               // predecessor tiles read per look-back round of a radix pass
 
 __device__ __forceinline__ uint32_t lanemask_lt() {
     uint32_t m;
@@ -314,27 +315,34 @@ __global__ __launch_bounds__(kSortThreads, 4) void k_onesweep(const uint32_t* __
     st_relaxed(my_lb, (tile == 0 ? kFlagPrefix : kFlagAgg) | tot);
     uint32_t excl = 0u;
     if (tile > 0) {
-        // look back four tiles per round of loads
+        // look back kLookBack tiles per round of loads
         int32_t j = (int32_t)tile - 1;
         uint32_t spins = 0u;
         bool done = false;
         while (!done) {
-            uint32_t w[4];
+            uint32_t w[kLookBack];
 #pragma unroll
-            for (int q = 0; q < 4; q++)
+            for (int q = 0; q < kLookBack; q++)
                 w[q] = j - q >= 0 ? ld_relaxed(lookback + (size_t)(j - q) * kRadix + d) : kFlagPrefix;
-            int q = 0;
-            for (; q < 4; q++) {
-                if ((w[q] & kFlagMask) == 0u) break;  // not published yet: poll it again
-                excl += w[q] & kValueMask;
-                if (w[q] & kFlagPrefix) {
-                    done = true;
-                    break;
+            int take = kLookBack;  // predecessors consumed this round
+            bool stop = false;
+#pragma unroll
+            for (int q = 0; q < kLookBack; q++) {
+                if (stop) continue;
+                if ((w[q] & kFlagMask) == 0u) {  // not published yet: poll it again
+                    take = q;
+                    stop = true;
+                } else {
+                    excl += w[q] & kValueMask;
+                    if (w[q] & kFlagPrefix) {
+                        done = true;
+                        stop = true;
+                    }
                 }
             }
             if (done) break;
-            j -= q;
-            if (q < 4) {
+            j -= take;
+            if (take < kLookBack) {
                 if (++spins > kSpinLimit) {
                     atomicOr(err, kErrTimeout);
                     break;
@@ -765,7 +773,7 @@ cudaError_t launch_merge(cudaStream_t s, const uint32_t* a_key, const uint32_t* 
     if (n == 0 || num_keys == 0) return cudaSuccess;
     const uint32_t tiles = merge_tiles(n);
     const uint32_t cap = kstart_chunk_cap(num_keys);
-    k_merge_path<<<(tiles + 1u + 255u) / 256u, 256, 0, s>>>(a_key, b_key, counts, n, tiles + 1u, split);
+    k_merge_path<<<(tiles + 1u + 7u) / 8u, 256, 0, s>>>(a_key, b_key, counts, n, tiles + 1u, split);  // a warp each
     cudaError_t e = cudaGetLastError();
     if (e == cudaSuccess) e = cudaMemsetAsync(chunk_count, 0, sizeof(uint32_t), s);
     if (e != cudaSuccess) return e;
