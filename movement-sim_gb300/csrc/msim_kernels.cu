@@ -429,8 +429,10 @@ __global__ void k_ranges(const uint32_t* __restrict__ sk, uint32_t n, uint32_t* 
 }
 
 // The query keeps the sorted positions of an entity's first kRegKeep neighbours in
-// shared memory; entities with more take list_overflow.
-constexpr int kRegKeep = 4;
+// shared memory; entities with more take list_overflow, which walks their tiles again
+// and holds up the whole warp.  At the 16 M workload 0.9 % of the entities have more
+// than 4 neighbours (a quarter of the warps would wait) and 0.001 % more than 8.
+constexpr int kRegKeep = 8;
 
 // Exact ascending list of the cap smallest ids of one entity, written by
 // insertion straight into its output slots; for the rare entities with more

@@ -405,22 +405,32 @@ __global__ __launch_bounds__(kQueryThreads) void k_query(const uint32_t* __restr
             if (lane >= (uint32_t)o) incl += y;
         }
         uint32_t* out = list + (size_t)(p >> 5) * 32u * cap + (incl - kept);
+        // the warp's largest kept list bounds the (warp-uniform) id fetch and insertion
+        const uint32_t wmax = __reduce_max_sync(FULL, count <= (uint32_t)kRegKeep ? count : 0u);
         if (count <= (uint32_t)kRegKeep) {  // every neighbour is kept: ids, sort, write
-            uint32_t keep[kRegKeep];
+            uint32_t id[kRegKeep];
+#pragma unroll
+            for (int i = 0; i < kRegKeep; i++) {  // all fetches of a lane in flight together
+                id[i] = 0xffffffffu;
+                if ((uint32_t)i < wmax) {
+                    const uint32_t s2 = (uint32_t)i < count ? sorted_slot[sh.keep[i][tid]] : n;
+                    id[i] = s2 < n ? slot_id[s2] : 0xffffffffu;
+                }
+            }
+            uint32_t keep[kRegKeep];  // ascending; unused slots hold 0xffffffff
+#pragma unroll
+            for (int i = 0; i < kRegKeep; i++) keep[i] = 0xffffffffu;
 #pragma unroll
             for (int i = 0; i < kRegKeep; i++) {
-                const uint32_t s2 = (uint32_t)i < count ? sorted_slot[sh.keep[i][tid]] : n;
-                keep[i] = s2 < n ? slot_id[s2] : 0xffffffffu;
+                if ((uint32_t)i >= wmax) continue;  // uniform
+                keep[kRegKeep - 1] = id[i];  // the last slot is free: at most i < kRegKeep are in
+#pragma unroll
+                for (int j = kRegKeep - 1; j > 0; j--) {
+                    const uint32_t lo = min(keep[j - 1], keep[j]), hi = max(keep[j - 1], keep[j]);
+                    keep[j - 1] = lo;
+                    keep[j] = hi;
+                }
             }
-#pragma unroll
-            for (int a = 0; a < kRegKeep; a++)
-#pragma unroll
-                for (int b = 0; b + 1 < kRegKeep - a; b++)
-                    if (keep[b] > keep[b + 1]) {
-                        const uint32_t t = keep[b];
-                        keep[b] = keep[b + 1];
-                        keep[b + 1] = t;
-                    }
 #pragma unroll
             for (int i = 0; i < kRegKeep; i++)
                 if ((uint32_t)i < kept) out[i] = keep[i];
