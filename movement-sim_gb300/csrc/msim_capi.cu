@@ -642,7 +642,11 @@ int msim_create(const msim_map* map, const msim_params* params, msim_ctx** out) 
     c->grid.ybands = (float)(1u << c->grid.ybits);
     c->passes = (2 * bits + c->grid.ybits + 7) / 8;
     c->num_keys = (size_t)1 << (2 * bits + c->grid.ybits);
-    c->resort = p.resort_interval ? p.resort_interval : 16u;
+    // entities move a small fraction of a tile per tick, so the slot order stays close
+    // to the sorted order for many ticks: measured at 16 M over 1000 ticks, 0.917 ms
+    // per tick re-ordering every 16 ticks, 0.895 every 64, 0.894 every 128 (the other
+    // kernels' times unchanged)
+    c->resort = p.resort_interval ? p.resort_interval : 64u;
     c->sort_tiles = (uint32_t)((c->n + kSortTile - 1) / kSortTile);
     if (c->sort_tiles == 0) c->sort_tiles = 1;
 
