@@ -323,15 +323,23 @@ def run_e2e(pkg, sim, cfg, n, nbr, world, steps):
         return max_over_ranks(time.perf_counter() - t0, world)
 
     dt = timed(fused)
+    # bytes back per step: in place (the same page-locked arrays in and out) the tick
+    # downloads positions and counts and writes the headings and RNG states that change
+    # into the arrays; counted here over one more tick
+    h0, r0 = head.array.copy(), rng.array.copy()
+    fused()
+    changed_head = int(np.count_nonzero(head.array != h0))
+    changed_rng = int(np.count_nonzero(np.any(rng.array != r0, axis=1)))
     dt_sep = timed(separate)
     h2d = n * (8 + 4 + 16 + 4)
-    d2h = n * (8 + 4 + 16 + (4 if nbr else 0))
+    d2h = n * (8 + (4 if nbr else 0)) + 4 * changed_head + 16 * changed_rng
     for b in (pos, head, rng, speed, cnt):
         b.free()
     return {"value": world * n * steps / dt, "unit": "entity-steps/s", "h2d_bytes_per_step": h2d,
             "d2h_bytes_per_step": d2h, "steps": steps, "ms_per_step": 1e3 * dt / steps,
-            "path": "msim_tick_host: page-locked host state in and out (pos, heading, rng, speed in; pos, heading, "
-                    "rng, neighbour counts out)",
+            "path": "msim_tick_host in place: page-locked host arrays for pos, heading, rng (in and out) and speed; "
+                    "positions and neighbour counts downloaded, the headings / RNG states that change "
+                    f"({changed_head} / {changed_rng} per tick) written into the arrays by the move kernel",
             "separate_calls": {"value": world * n * steps / dt_sep, "ms_per_step": 1e3 * dt_sep / steps,
                                "path": "msim_set_entities + msim_step(1) + msim_get_state + msim_get_neighbours"}}
 

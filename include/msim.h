@@ -199,8 +199,11 @@ int msim_get_neighbours(msim_ctx* ctx, uint32_t* count, uint32_t* idx);
  * buffers (msim_host_alloc) the copies run asynchronously; pageable ones work too.
  * in_speed may be NULL (1.4 m per tick at dt = 1); any output may be NULL; out_count
  * and out_idx need MSIM_STEP_NEIGHBOURS.  in_pos / out_pos (and heading, rng) may be
- * the same arrays: a chunk has been uploaded before its download writes it.
- * Synchronous.  A heading naming a road out of
+ * the same arrays: a chunk has been uploaded before its download writes it.  When
+ * heading and rng are each one page-locked array for input and output (in place),
+ * only the headings and RNG states that change (entities at a road end) are written
+ * back, by the move kernel through the arrays' device mapping, and just positions
+ * and counts are downloaded.  Synchronous.  A heading naming a road out of
  * range gives MSIM_ERR_OOB and keeps the previous state (as msim_set_entities);
  * the outputs are then undefined. */
 int msim_tick_host(msim_ctx* ctx, const float* in_pos, const uint32_t* in_heading, const uint32_t* in_rng,

@@ -296,6 +296,17 @@ StepLaunch step_args(msim_ctx* c, uint32_t ticks, bool key) {
     return a;
 }
 
+// Device address of page-locked host memory (registered or from cudaMallocHost), or
+// nullptr for any other pointer.
+void* mapped_host(const void* p) {
+    cudaPointerAttributes at{};
+    if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return at.type == cudaMemoryTypeHost ? at.devicePointer : nullptr;
+}
+
 // The main stream waits for the queries still running on qstream that read index
 // buffer set b (wait_reads) or any set (join_query).
 int wait_reads(msim_ctx* c, int b) {
@@ -905,6 +916,23 @@ int msim_tick_host(msim_ctx* c, const float* in_pos, const uint32_t* in_heading,
     // followed by one tick): the new state goes to the same slots.
     const bool old_slots_identity = c->slots_identity;
     const bool use_inc = nbr && c->incremental && c->sorted_key && c->slots_identity;
+    // In place (the same page-locked arrays for heading and RNG in and out): they
+    // already hold every value the tick leaves unchanged, so the move kernel writes the
+    // headings and RNG states that change (entities at a road end, a few per thousand
+    // per tick) straight into them through their device mapping, and only positions
+    // are downloaded.
+    uint32_t* dev_head = nullptr;
+    uint4* dev_rng = nullptr;
+    if (out_heading && static_cast<const void*>(out_heading) == static_cast<const void*>(in_heading) && out_rng &&
+        static_cast<const void*>(out_rng) == static_cast<const void*>(in_rng)) {
+        dev_head = static_cast<uint32_t*>(mapped_host(out_heading));
+        dev_rng = static_cast<uint4*>(mapped_host(out_rng));
+        if (!dev_head || !dev_rng || (reinterpret_cast<uintptr_t>(dev_rng) & 15u)) {
+            dev_head = nullptr;
+            dev_rng = nullptr;
+        }
+    }
+    const bool in_place = dev_head != nullptr;
     CK(cudaMemsetAsync(c->check, 0xff, sizeof(uint32_t), c->stream), "memset check");
     if (nbr && !use_inc) CK(cudaMemsetAsync(c->hist, 0, sizeof(uint32_t) * kMaxPasses * kRadix, c->stream), "memset hist");
     CK(cudaEventRecord(c->ev_start, c->stream), "cudaEventRecord");
@@ -941,6 +969,9 @@ int msim_tick_host(msim_ctx* c, const float* in_pos, const uint32_t* in_heading,
             a.key = nbr ? c->key + lo : nullptr;
             if (use_inc) a.hist = nullptr;  // the changed keys' digits are counted by k_mark
             a.blocks = std::min<int>(c->step_blocks, (int)((cnt + kStepThreads - 1) / kStepThreads));
+            a.host_head = dev_head;
+            a.host_rng = dev_rng;
+            a.id_base = lo;
             CK(launch_step(c->stream, a), "k_step");
         }
         CK(cudaEventRecord(c->ev_moved[k], c->stream), "cudaEventRecord");
@@ -949,6 +980,7 @@ int msim_tick_host(msim_ctx* c, const float* in_pos, const uint32_t* in_heading,
             CK(cudaMemcpyAsync(out_pos + 2 * (size_t)lo, s.pos + lo, sizeof(float2) * cnt, cudaMemcpyDeviceToHost,
                                c->down),
                "download pos");
+        if (in_place) continue;  // headings and RNG states: written by the move kernel
         if (out_heading)
             CK(cudaMemcpyAsync(out_heading + lo, s.head + lo, sizeof(uint32_t) * cnt, cudaMemcpyDeviceToHost, c->down),
                "download heading");

@@ -183,8 +183,14 @@ __global__ __launch_bounds__(kStepThreads) void k_step(StepLaunch a) {
                 for (uint32_t t = 0; t < a.ticks; t++)
                     step_entity<RNG>(a.map, a.dt, sp[u], p[u], h[u], r, rl, rd, a.st.rng + sl[u], a.err);
                 a.st.pos[sl[u]] = p[u];
-                if (h[u] != h0[u]) a.st.head[sl[u]] = h[u];
-                if (rd) a.st.rng[sl[u]] = r;
+                if (h[u] != h0[u]) {
+                    a.st.head[sl[u]] = h[u];
+                    if (a.host_head) a.host_head[a.id_base + sl[u]] = h[u];  // the caller's copy, by id
+                }
+                if (rd) {
+                    a.st.rng[sl[u]] = r;
+                    if (a.host_rng) a.host_rng[a.id_base + sl[u]] = r;
+                }
             }
             if (KEY) {
                 key[u] = tile_key(a.grid, p[u], s_morton);

@@ -41,6 +41,13 @@ struct StepLaunch {
     uint32_t passes;
     uint32_t* err;
     int blocks;           // grid size (grid-stride loop)
+    // Host round trip with the caller's arrays both input and output: the headings and
+    // RNG states that change are also written to them (device-mapped page-locked host
+    // memory, indexed by id_base + slot; slot = entity id there), so only positions
+    // need a download.  nullptr otherwise.
+    uint32_t* host_head = nullptr;
+    uint4* host_rng = nullptr;
+    uint32_t id_base = 0;
 };
 
 cudaError_t launch_init_entities(cudaStream_t s, const DeviceMap& m, EntityState st, uint32_t n,

@@ -153,3 +153,46 @@ def test_host_ticks_with_host_edits_and_mixed_calls(msim, orc):
             assert np.array_equal(got["count"], ocnt), f"counts differ at tick {t + 1}"
             state = {"pos": got["pos"].copy(), "heading": got["heading"].copy(), "rng": got["rng"].copy(),
                      "speed": speed}
+
+
+@pytest.mark.parametrize("pinned", [True, False])
+def test_tick_host_in_place(msim, orc, pinned):
+    """The same arrays as input and output: with page-locked arrays only positions are
+    downloaded and the changed headings / RNG states are written into the arrays by
+    the move kernel; with pageable ones everything is downloaded.  Either way the
+    arrays hold the oracle's state after every tick, also when the host edits them."""
+    road_map = msim.RoadMap.lattice(32, 6)
+    n = 200_000
+    rs = np.random.default_rng(3)
+    with msim.Simulation(road_map, n, rng="xorshift128", dt=0.1, radius=2.0, cap=8, index="incremental") as sim:
+        sim.init_entities(9, placement="fraction", speed=(1.0, 1.6))
+        st = sim.get_state()
+        bufs = {}
+        if pinned:
+            bufs = {"pos": msim.PinnedBuffer((n, 2), np.float32), "heading": msim.PinnedBuffer(n, np.uint32),
+                    "rng": msim.PinnedBuffer((n, 4), np.uint32), "count": msim.PinnedBuffer(n, np.uint32)}
+            state = {k: b.array for k, b in bufs.items()}
+            for k in ("pos", "heading", "rng"):
+                state[k][...] = st[k]
+        else:
+            state = {k: st[k].copy() for k in ("pos", "heading", "rng")}
+            state["count"] = np.empty(n, np.uint32)
+        state["speed"] = st["speed"]
+        pos, head, rng, speed = st["pos"].copy(), st["heading"].copy(), st["rng"].copy(), st["speed"].copy()
+        for t in range(8):
+            if t == 4:  # host edits between ticks
+                who = rs.choice(n, 5000, replace=False)
+                roads = rs.integers(0, road_map.num_roads, who.size)
+                for arr in (state["pos"], pos):
+                    arr[who] = road_map.road_pos[roads, :2]
+                for arr in (state["heading"], head):
+                    arr[who] = roads.astype(np.uint32) | np.uint32(0x80000000)
+            sim.tick_host(state, neighbours=True, out=state)
+            orc.step(road_map.road_pos, road_map.road_conn, road_map.connections, pos, head, rng, speed, 0, 0.1, 1,
+                     threads=8)
+            _same_state(state, {"pos": pos, "heading": head, "rng": rng}, f"at tick {t + 1}")
+            ocnt, _, _ = orc.neighbours(pos, 2.0, 8, threads=8, with_idx=False)
+            assert np.array_equal(state["count"], ocnt), f"counts differ at tick {t + 1}"
+        assert np.any(rng != st["rng"])  # road-end draws happened, so the RNG write-back was exercised
+        for b in bufs.values():
+            b.free()
