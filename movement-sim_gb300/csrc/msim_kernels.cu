@@ -11,6 +11,10 @@
 //   k_kstart    key-start table: first sorted position of every key (tile + band)
 //   k_query     radius neighbour query (random_move.comp:541-719 semantics: the
 //               pair predicate of :551-562), count + the cap smallest ids
+// From 4 M entities the sort is replaced by an incremental update of the previous
+// order (msim_incsort.cuh): k_mark splits it by changed keys, k_onesweep sorts the
+// changed entries, k_merge_path + k_merge merge them back and write the key-start
+// table and the sorted positions.
 // Every few ticks k_permute re-orders the entity state by the sorted order so
 // that the step and the query keep reading memory almost sequentially.
 #include <cstdio>
@@ -594,7 +598,6 @@ inline unsigned blocks_for(uint32_t n, unsigned threads) { return (unsigned)((n 
 
 }  // namespace
 
-int query_smem_bytes(uint32_t) { return 0; }  // the query keeps its lists in registers
 
 cudaError_t configure_kernels(uint32_t) { return cudaSuccess; }
 

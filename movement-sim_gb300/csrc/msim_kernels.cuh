@@ -108,7 +108,6 @@ cudaError_t launch_export_neighbours(cudaStream_t s, const uint32_t* sorted_slot
 cudaError_t launch_export_aos(cudaStream_t s, const DeviceMap& m, EntityState st, uint32_t n, float dt,
                               const uint32_t* sorted_slot, const uint32_t* count, void* out);
 
-int query_smem_bytes(uint32_t cap);
 cudaError_t configure_kernels(uint32_t cap);
 int step_blocks_for(int device, uint32_t n);
 
