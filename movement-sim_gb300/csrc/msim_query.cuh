@@ -234,7 +234,9 @@ __global__ __launch_bounds__(256) void k_kstart_search(const uint32_t* __restric
 // keeps the candidate's sorted position; ids are looked up only for those.  An
 // entity with more than kRegKeep neighbours redoes an exact pass into its output
 // slots.  The predicate is symmetric (fl(a - b) = -fl(b - a)), so the pair count is
-// half the sum of the counts.  Each warp writes its lists contiguously at
+// half the sum of the counts, and a pair of entities of the same warp (most pairs:
+// consecutive sorted entities share their band runs) is tested once, by the lower
+// lane, which credits both.  Each warp writes its lists contiguously at
 // warp * 32 * cap and adds its count sum to one of kPairBins counters; the kernel has
 // no block-wide barrier.
 constexpr uint32_t kRuns = 4;                  // runs per lane and round
@@ -250,10 +252,28 @@ struct QueryShared {
 };
 
 template <bool LIST>
-__device__ __forceinline__ void query_runs(const uint32_t (&lo)[kRuns], const uint32_t (&len)[kRuns], uint32_t lane,
-                                           uint32_t warp, uint32_t pwarp, QueryShared& sh,
+__device__ __forceinline__ void query_runs(const uint32_t (&lo_in)[kRuns], const uint32_t (&len_in)[kRuns],
+                                           uint32_t lane, uint32_t warp, uint32_t pwarp, QueryShared& sh,
                                            const float2* __restrict__ sorted_pos, const TileGrid& g) {
     constexpr uint32_t FULL = 0xffffffffu;
+    // A pair of entities of this warp is tested once, by the lower lane, which credits
+    // both (the predicate is symmetric, and an in-range pair lies in both entities'
+    // runs).  So a lane skips the warp's positions up to its own: a run that starts at
+    // or after the warp's first position starts after the owner instead (a run that
+    // starts before it is kept whole; the loop skips those positions).  At 16 M about
+    // 4.7 of the 5.3 candidates of an entity lie in its own warp.
+    uint32_t lo[kRuns], len[kRuns];
+#pragma unroll
+    for (uint32_t k = 0; k < kRuns; k++) {
+        lo[k] = lo_in[k];
+        len[k] = len_in[k];
+        if (len[k] && lo[k] >= pwarp) {
+            const uint32_t hi = lo[k] + len[k];
+            const uint32_t from = lo[k] > pwarp + lane ? lo[k] : pwarp + lane + 1u;
+            lo[k] = from;
+            len[k] = hi > from ? hi - from : 0u;
+        }
+    }
     uint32_t flat = 0, nr = 0;
 #pragma unroll
     for (uint32_t k = 0; k < kRuns; k++) {
@@ -296,17 +316,25 @@ __device__ __forceinline__ void query_runs(const uint32_t (&lo)[kRuns], const ui
         if (i >= total) continue;
         const uint32_t q = sh.rq[warp][run] + i;
         const uint32_t owner = sh.rown[warp][run];
-        if (q == pwarp + owner) continue;  // the owner itself
+        const uint32_t other = q - pwarp;  // the candidate's lane when it is in this warp
+        if (other <= owner) continue;      // the owner itself or a lower lane: tested from there
         const uint32_t ot = warp * 32u + owner;
         if (!in_range_fast(sorted_pos[q], sh.me[ot], g.radius, g.d2_limit)) continue;
         const uint32_t c = atomicAdd(&sh.cnt[ot], 1u);
         if (LIST && c < (uint32_t)kRegKeep) sh.keep[c][ot] = q;  // sorted position; the id comes later
+        if (other < 32u) {  // a higher lane of this warp: the pair counts for it too
+            const uint32_t om = warp * 32u + other;
+            const uint32_t c2 = atomicAdd(&sh.cnt[om], 1u);
+            if (LIST && c2 < (uint32_t)kRegKeep) sh.keep[c2][om] = pwarp + owner;
+        }
     }
     __syncwarp();  // before the run list is rewritten
 }
 
+// 16 blocks (64 warps) per SM: at 40 registers (12 blocks) the symmetric pair loop
+// gained nothing (0.435 against 0.437 ms at 16 M), at 32 it takes 0.395.
 template <bool LIST>
-__global__ __launch_bounds__(kQueryThreads) void k_query(const uint32_t* __restrict__ kstart,
+__global__ __launch_bounds__(kQueryThreads, 16) void k_query(const uint32_t* __restrict__ kstart,
                                                          const uint32_t* __restrict__ sorted_slot,
                                                          const float2* __restrict__ sorted_pos,
                                                          const uint32_t* __restrict__ slot_id, TileGrid g,
