@@ -68,8 +68,10 @@ struct msim_ctx {
     uint32_t* sv[2] = {nullptr, nullptr};
     uint32_t* hist = nullptr;
     uint32_t* digit_off = nullptr;
-    uint32_t* lookback = nullptr;
+    uint32_t* lookback = nullptr;   // kMaxPasses regions of sort_region words, chained (see sweep_chain)
     uint32_t* tickets = nullptr;
+    uint32_t* sort_dirty = nullptr; // per region: look-back words its last pass published
+    size_t sort_region = 0;
     // The index the query reads (current buffer set).  Two sets, paired with the two
     // sorted-slot buffers: a tick's merge writes the set the previous tick's query does
     // not read, so that query overlaps the next tick up to its merge.
@@ -83,7 +85,6 @@ struct msim_ctx {
     uint32_t* kstart_chunk_count_b[2] = {nullptr, nullptr};
     int ib = 0;  // current index buffer set
     size_t num_keys = 0;
-    uint32_t sort_tiles = 0;
     const uint32_t* sorted_key = nullptr;
     const uint32_t* sorted_slot = nullptr;
     bool have_sort = false;
@@ -330,6 +331,26 @@ void use_index_buffers(msim_ctx* c, int b) {
     c->kstart_chunk_count = c->kstart_chunk_count_b[b];
 }
 
+// Radix passes over the look-back regions: with two or more passes each pass
+// clears the next one's region and ticket (the regions start zeroed at creation),
+// so no memset runs between them; a single pass clears its own before it runs.
+SweepChain sweep_chain(msim_ctx* c, uint32_t ps) {
+    SweepChain ch;
+    const uint32_t nx = (ps + 1u) % c->passes;
+    ch.next_lookback = c->lookback + nx * c->sort_region;
+    ch.next_ticket = c->tickets + nx;
+    ch.next_dirty = c->sort_dirty + nx;
+    ch.my_dirty = c->sort_dirty + ps;
+    return ch;
+}
+
+int clear_unchained(msim_ctx* c) {
+    if (c->passes >= 2) return MSIM_OK;
+    CK(cudaMemsetAsync(c->lookback, 0, sizeof(uint32_t) * c->sort_region, c->stream), "memset lookback");
+    CK(cudaMemsetAsync(c->tickets, 0, sizeof(uint32_t) * kMaxPasses, c->stream), "memset tickets");
+    return MSIM_OK;
+}
+
 int sort_keys(msim_ctx* c);
 
 // key + histogram (of the current positions, or after one move tick) + radix sort
@@ -348,18 +369,18 @@ int sort_keys(msim_ctx* c) {
         Prof p(c, K_HIST_SCAN);
         CK(launch_hist_scan(c->stream, c->hist, c->digit_off, c->passes), "k_hist_scan");
     }
-    CK(cudaMemsetAsync(c->lookback, 0, sizeof(uint32_t) * (size_t)c->passes * c->sort_tiles * kRadix, c->stream),
-       "memset lookback");
-    CK(cudaMemsetAsync(c->tickets, 0, sizeof(uint32_t) * kMaxPasses, c->stream), "memset tickets");
-    int rc = join_query(c);  // the passes rewrite the sorted slots the last query reads
+    int rc = clear_unchained(c);
+    if (rc != MSIM_OK) return rc;
+    rc = join_query(c);  // the passes rewrite the sorted slots the last query reads
     if (rc != MSIM_OK) return rc;
     for (uint32_t ps = 0; ps < c->passes; ps++) {
         const uint32_t* kin = ps == 0 ? c->key : c->sk[(ps - 1) & 1];
         const uint32_t* vin = ps == 0 ? nullptr : c->sv[(ps - 1) & 1];
+        const SweepChain ch = sweep_chain(c, ps);
         Prof p(c, K_SORT_PASS);
         CK(launch_onesweep(c->stream, kin, vin, c->sk[ps & 1], c->sv[ps & 1], c->n, 8u * ps,
-                           c->digit_off + ps * kRadix, c->lookback + (size_t)ps * c->sort_tiles * kRadix,
-                           c->tickets + ps, c->err),
+                           c->digit_off + ps * kRadix, c->lookback + ps * c->sort_region, c->tickets + ps, c->err,
+                           nullptr, c->passes >= 2 ? &ch : nullptr),
            "k_onesweep");
     }
     c->sorted_key = c->sk[(c->passes - 1) & 1];
@@ -435,21 +456,21 @@ int incremental_update(msim_ctx* c) {
         Prof p(c, K_HIST_SCAN);
         CK(launch_hist_scan(c->stream, c->hist, c->digit_off, c->passes), "k_hist_scan");
     }
-    CK(cudaMemsetAsync(c->lookback, 0, sizeof(uint32_t) * (size_t)c->passes * c->sort_tiles * kRadix, c->stream),
-       "memset lookback");
-    CK(cudaMemsetAsync(c->tickets, 0, sizeof(uint32_t) * kMaxPasses, c->stream), "memset tickets");
+    int rc = clear_unchained(c);
+    if (rc != MSIM_OK) return rc;
     for (uint32_t ps = 0; ps < c->passes; ps++) {  // stable radix sort of the changed entries
+        const SweepChain ch = sweep_chain(c, ps);
         Prof p(c, K_SORT_PASS);
         CK(launch_onesweep(c->stream, c->b_key[ps & 1], c->b_val[ps & 1], c->b_key[(ps + 1) & 1],
                            c->b_val[(ps + 1) & 1], c->n, 8u * ps, c->digit_off + ps * kRadix,
-                           c->lookback + (size_t)ps * c->sort_tiles * kRadix, c->tickets + ps, c->err,
-                           c->ab_counts + 1),
+                           c->lookback + ps * c->sort_region, c->tickets + ps, c->err, c->ab_counts + 1,
+                           c->passes >= 2 ? &ch : nullptr),
            "k_onesweep");
     }
     // The merge writes the sorted slots and index buffer set the previous tick's query
     // does not read (that query may still run); it waits for the query before that.
     const int out = c->sorted_key == c->sk[0] ? 1 : 0;
-    int rc = wait_reads(c, out);
+    rc = wait_reads(c, out);
     if (rc != MSIM_OK) return rc;
     use_index_buffers(c, out);
     {
@@ -658,8 +679,7 @@ int msim_create(const msim_map* map, const msim_params* params, msim_ctx** out) 
     // per tick re-ordering every 16 ticks, 0.895 every 64, 0.894 every 128 (the other
     // kernels' times unchanged)
     c->resort = p.resort_interval ? p.resort_interval : 64u;
-    c->sort_tiles = (uint32_t)((c->n + kSortTile - 1) / kSortTile);
-    if (c->sort_tiles == 0) c->sort_tiles = 1;
+    c->sort_region = sort_lookback_words(c->n);
 
     // ---- device buffers ----
     const size_t n = c->n;
@@ -674,7 +694,8 @@ int msim_create(const msim_map* map, const msim_params* params, msim_ctx** out) 
     }
     if ((rc = dalloc(c, &c->key, n)) || (rc = dalloc(c, &c->hist, (size_t)kMaxPasses * kRadix)) ||
         (rc = dalloc(c, &c->digit_off, (size_t)kMaxPasses * kRadix)) ||
-        (rc = dalloc(c, &c->lookback, (size_t)kMaxPasses * c->sort_tiles * kRadix)) ||
+        (rc = dalloc(c, &c->lookback, (size_t)kMaxPasses * c->sort_region)) ||
+        (rc = dalloc(c, &c->sort_dirty, (size_t)kMaxPasses)) ||
         (rc = dalloc(c, &c->tickets, (size_t)kMaxPasses)) || (rc = dalloc(c, &c->a_key, n)) || (rc = dalloc(c, &c->a_val, n)) ||
         (rc = dalloc(c, &c->b_key[0], n)) || (rc = dalloc(c, &c->b_key[1], n)) || (rc = dalloc(c, &c->b_val[0], n)) ||
         (rc = dalloc(c, &c->b_val[1], n)) || (rc = dalloc(c, &c->ab_counts, 2)) ||
@@ -704,6 +725,9 @@ int msim_create(const msim_map* map, const msim_params* params, msim_ctx** out) 
     if (e == cudaSuccess) e = cudaMemcpy(c->conn, conn.data(), sizeof(uint32_t) * (c->C + 1), cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemsetAsync(c->err, 0, sizeof(uint32_t), c->stream);
     if (e == cudaSuccess) e = cudaMemsetAsync(c->sorted_dev, 0, sizeof(unsigned long long), c->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(c->lookback, 0, sizeof(uint32_t) * kMaxPasses * c->sort_region, c->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(c->tickets, 0, sizeof(uint32_t) * kMaxPasses, c->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(c->sort_dirty, 0, sizeof(uint32_t) * kMaxPasses, c->stream);
     for (int b = 0; b < 2 && e == cudaSuccess; b++) {
         e = cudaMemsetAsync(c->st[b].pos, 0, sizeof(float2) * std::max<size_t>(n, 1), c->stream);
         if (e == cudaSuccess) e = cudaMemsetAsync(c->st[b].head, 0, sizeof(uint32_t) * std::max<size_t>(n, 1), c->stream);

@@ -12,6 +12,7 @@ namespace msim {
 constexpr int kSortThreads = 256;
 constexpr int kSortRows = 16;                               // items per thread
 constexpr uint32_t kSortTile = kSortThreads * kSortRows;    // 4096 items per block
+constexpr int kSortRowsDev = 4;                             // the same, for passes with a device-side count
 constexpr uint32_t kRadix = 256;                            // 8-bit digits
 constexpr int kMaxPasses = 3;                               // keys up to 24 bits
 constexpr int kQueryThreads = 128;
@@ -55,10 +56,23 @@ cudaError_t launch_init_entities(cudaStream_t s, const DeviceMap& m, EntityState
                                  float smax);
 cudaError_t launch_step(cudaStream_t s, const StepLaunch& a);
 cudaError_t launch_hist_scan(cudaStream_t s, const uint32_t* hist, uint32_t* offsets, uint32_t passes);
+// Look-back bookkeeping that lets consecutive radix passes run without a memset
+// between them: before its tiles a pass zeroes next_lookback[0, *next_dirty) and
+// *next_ticket, and sets *my_dirty to the look-back words it publishes itself.  The
+// look-back words and tickets start zeroed, and every pass over them is chained.
+struct SweepChain {
+    uint32_t* next_lookback = nullptr;
+    uint32_t* next_ticket = nullptr;
+    const uint32_t* next_dirty = nullptr;
+    uint32_t* my_dirty = nullptr;
+};
+// Look-back words one pass over n items may publish (either tile size).
+size_t sort_lookback_words(uint32_t n);
 cudaError_t launch_onesweep(cudaStream_t s, const uint32_t* keys_in, const uint32_t* vals_in,
                             uint32_t* keys_out, uint32_t* vals_out, uint32_t n, uint32_t shift,
                             const uint32_t* digit_offset, uint32_t* lookback, uint32_t* ticket,
-                            uint32_t* err, const uint32_t* n_dev = nullptr);  // n_dev: count on the device (<= n)
+                            uint32_t* err, const uint32_t* n_dev = nullptr,  // n_dev: count on the device (<= n)
+                            const SweepChain* chain = nullptr);
 cudaError_t launch_ranges(cudaStream_t s, const uint32_t* sorted_key, uint32_t n, uint2* ranges, uint32_t num_keys,
                           uint32_t ybits = 0);
 // Key-start table of sorted keys (num_keys + 1 entries).  chunks / chunk_count
