@@ -67,7 +67,6 @@ KERNEL_BYTES = {
     "k_query": lambda k: 12 + 4 * k,       # own pos 8 + count 4 + kept ids
     "k_permute": lambda k: 72,             # 36-byte state read + write
     "k_step_multi": lambda k: B_STEP,      # per tick
-    "k_hist_scan": lambda k: 0,
 }
 
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per entity and launch of

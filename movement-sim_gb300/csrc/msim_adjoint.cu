@@ -521,7 +521,6 @@ struct msim_adj {
     uint32_t* sk[2] = {nullptr, nullptr};
     uint32_t* sv[2] = {nullptr, nullptr};
     uint32_t* hist = nullptr;
-    uint32_t* digit_off = nullptr;
     uint32_t* lookback = nullptr;
     uint32_t* tickets = nullptr;
     uint32_t* kstart = nullptr;
@@ -688,7 +687,6 @@ int msim_adj_create(const msim_map* map, const msim_adj_params* params, msim_adj
         (rc = aalloc(a, &a->rec_val, a->rec_count)) || (rc = aalloc(a, &a->sk[0], a->rec_count)) ||
         (rc = aalloc(a, &a->sk[1], a->rec_count)) || (rc = aalloc(a, &a->sv[0], a->rec_count)) ||
         (rc = aalloc(a, &a->sv[1], a->rec_count)) || (rc = aalloc(a, &a->hist, (size_t)kMaxPasses * kRadix)) ||
-        (rc = aalloc(a, &a->digit_off, (size_t)kMaxPasses * kRadix)) ||
         (rc = aalloc(a, &a->lookback, (size_t)kMaxPasses * a->rec_tiles * kRadix)) ||
         (rc = aalloc(a, &a->tickets, (size_t)kMaxPasses)) || (rc = aalloc(a, &a->kstart, (size_t)a->R + 2)) ||
         (rc = aalloc(a, &a->err, 1)) || (rc = aalloc(a, &a->perm, n)))
@@ -869,7 +867,6 @@ int msim_adj_backward(msim_adj* a, float* d_grad_speed, float* d_grad_factor) {
     ACK(cudaMemsetAsync(a->hist, 0, sizeof(uint32_t) * kMaxPasses * kRadix, a->stream), "memset hist");
     k_adj_hist<<<1024, 256, 0, a->stream>>>(a->rec_road, a->rec_count, a->passes, a->hist);
     ACK(cudaGetLastError(), "k_adj_hist");
-    ACK(launch_hist_scan(a->stream, a->hist, a->digit_off, a->passes), "k_hist_scan");
     ACK(cudaMemsetAsync(a->lookback, 0, sizeof(uint32_t) * (size_t)a->passes * a->rec_tiles * kRadix, a->stream),
         "memset lookback");
     ACK(cudaMemsetAsync(a->tickets, 0, sizeof(uint32_t) * kMaxPasses, a->stream), "memset tickets");
@@ -877,7 +874,7 @@ int msim_adj_backward(msim_adj* a, float* d_grad_speed, float* d_grad_factor) {
         const uint32_t* kin = ps == 0 ? a->rec_road : a->sk[(ps - 1) & 1];
         const uint32_t* vin = ps == 0 ? nullptr : a->sv[(ps - 1) & 1];
         ACK(launch_onesweep(a->stream, kin, vin, a->sk[ps & 1], a->sv[ps & 1], total, 8u * ps,
-                            a->digit_off + ps * kRadix, a->lookback + (size_t)ps * a->rec_tiles * kRadix,
+                            a->hist + ps * kRadix, a->lookback + (size_t)ps * a->rec_tiles * kRadix,
                             a->tickets + ps, a->err),
             "k_onesweep");
     }

@@ -26,7 +26,6 @@ enum KernelId : uint32_t {
     K_INIT = 0,
     K_STEP,        // one tick + key + digit histogram (neighbour ticks)
     K_STEP_MULTI,  // several move-only ticks per launch
-    K_HIST_SCAN,
     K_SORT_PASS,
     K_KSTART,
     K_QUERY,
@@ -36,9 +35,9 @@ enum KernelId : uint32_t {
     K_MERGE,  // merge + key-start table + sorted positions
     K_COUNT
 };
-static const char* const kKernelNames[K_COUNT] = {"k_init",   "k_step",    "k_step_multi", "k_hist_scan",
-                                                  "k_onesweep", "k_kstart", "k_query",     "k_permute",
-                                                  "k_export", "k_mark",    "k_merge"};
+static const char* const kKernelNames[K_COUNT] = {"k_init",   "k_step",   "k_step_multi", "k_onesweep",
+                                                  "k_kstart", "k_query",  "k_permute",    "k_export",
+                                                  "k_mark",   "k_merge"};
 
 // msim_tick_host: at most this many chunks, each at least kHostChunkMin entities
 constexpr uint32_t kHostChunks = 8;
@@ -67,7 +66,6 @@ struct msim_ctx {
     uint32_t* sk[2] = {nullptr, nullptr};
     uint32_t* sv[2] = {nullptr, nullptr};
     uint32_t* hist = nullptr;
-    uint32_t* digit_off = nullptr;
     uint32_t* lookback = nullptr;   // kMaxPasses regions of sort_region words, chained (see sweep_chain)
     uint32_t* tickets = nullptr;
     uint32_t* sort_dirty = nullptr; // per region: look-back words its last pass published
@@ -365,10 +363,6 @@ int sort_entities(msim_ctx* c, uint32_t move_ticks) {
 
 // radix sort of (key, slot) for keys and digit counts already in c->key / c->hist
 int sort_keys(msim_ctx* c) {
-    {
-        Prof p(c, K_HIST_SCAN);
-        CK(launch_hist_scan(c->stream, c->hist, c->digit_off, c->passes), "k_hist_scan");
-    }
     int rc = clear_unchained(c);
     if (rc != MSIM_OK) return rc;
     rc = join_query(c);  // the passes rewrite the sorted slots the last query reads
@@ -379,7 +373,7 @@ int sort_keys(msim_ctx* c) {
         const SweepChain ch = sweep_chain(c, ps);
         Prof p(c, K_SORT_PASS);
         CK(launch_onesweep(c->stream, kin, vin, c->sk[ps & 1], c->sv[ps & 1], c->n, 8u * ps,
-                           c->digit_off + ps * kRadix, c->lookback + ps * c->sort_region, c->tickets + ps, c->err,
+                           c->hist + ps * kRadix, c->lookback + ps * c->sort_region, c->tickets + ps, c->err,
                            nullptr, c->passes >= 2 ? &ch : nullptr),
            "k_onesweep");
     }
@@ -452,17 +446,13 @@ int incremental_update(msim_ctx* c) {
            "k_mark");
         c->index_updates++;
     }
-    {
-        Prof p(c, K_HIST_SCAN);
-        CK(launch_hist_scan(c->stream, c->hist, c->digit_off, c->passes), "k_hist_scan");
-    }
     int rc = clear_unchained(c);
     if (rc != MSIM_OK) return rc;
     for (uint32_t ps = 0; ps < c->passes; ps++) {  // stable radix sort of the changed entries
         const SweepChain ch = sweep_chain(c, ps);
         Prof p(c, K_SORT_PASS);
         CK(launch_onesweep(c->stream, c->b_key[ps & 1], c->b_val[ps & 1], c->b_key[(ps + 1) & 1],
-                           c->b_val[(ps + 1) & 1], c->n, 8u * ps, c->digit_off + ps * kRadix,
+                           c->b_val[(ps + 1) & 1], c->n, 8u * ps, c->hist + ps * kRadix,
                            c->lookback + ps * c->sort_region, c->tickets + ps, c->err, c->ab_counts + 1,
                            c->passes >= 2 ? &ch : nullptr),
            "k_onesweep");
@@ -693,7 +683,6 @@ int msim_create(const msim_map* map, const msim_params* params, msim_ctx** out) 
             return bail(rc);
     }
     if ((rc = dalloc(c, &c->key, n)) || (rc = dalloc(c, &c->hist, (size_t)kMaxPasses * kRadix)) ||
-        (rc = dalloc(c, &c->digit_off, (size_t)kMaxPasses * kRadix)) ||
         (rc = dalloc(c, &c->lookback, (size_t)kMaxPasses * c->sort_region)) ||
         (rc = dalloc(c, &c->sort_dirty, (size_t)kMaxPasses)) ||
         (rc = dalloc(c, &c->tickets, (size_t)kMaxPasses)) || (rc = dalloc(c, &c->a_key, n)) || (rc = dalloc(c, &c->a_val, n)) ||

@@ -5,9 +5,9 @@
 //   k_step      move every entity one tick (random_move.comp:869-874), write its
 //               tile Morton key and count the key's radix digits (warp-aggregated
 //               by ballot over runs of equal digits, one shared atomic per run)
-//   k_hist_scan exclusive offsets of each digit pass
 //   k_onesweep  one stable LSD radix pass per 8-bit digit (decoupled look-back,
-//               warp-level multi-split ranking with __match_any_sync)
+//               warp-level multi-split ranking with __match_any_sync; every block
+//               scans the pass's digit counts into offsets itself)
 //   k_kstart    key-start table: first sorted position of every key (tile + band)
 //   k_query     radius neighbour query (random_move.comp:541-719 semantics: the
 //               pair predicate of :551-562), count + the cap smallest ids
@@ -216,14 +216,6 @@ __global__ __launch_bounds__(kStepThreads) void k_step(StepLaunch a) {
     }
 }
 
-__global__ __launch_bounds__(kRadix) void k_hist_scan(const uint32_t* hist, uint32_t* off, uint32_t passes) {
-    __shared__ uint32_t s_warp[kRadix / 32 + 1];
-    for (uint32_t ps = 0; ps < passes; ps++) {
-        uint32_t v = hist[ps * kRadix + threadIdx.x];
-        off[ps * kRadix + threadIdx.x] = block_exclusive_scan<kRadix>(v, s_warp, nullptr);
-    }
-}
-
 // One stable LSD radix pass over 8 bits of the key (Adinets & Merrill,
 // "Onesweep", 2022).  Blocks take tiles in launch order through an atomic ticket,
 // rank their ROWS x 256 items with warp-level multi-split (__match_any_sync) into
@@ -253,12 +245,13 @@ __global__ __launch_bounds__(kSortThreads, 4) void k_onesweep(const uint32_t* __
                                                               uint32_t* __restrict__ keys_out,
                                                               uint32_t* __restrict__ vals_out, uint32_t n,
                                                               uint32_t shift,
-                                                              const uint32_t* __restrict__ digit_offset,
+                                                              const uint32_t* __restrict__ digit_count,
                                                               uint32_t* lookback, uint32_t* ticket, uint32_t* err,
                                                               const uint32_t* __restrict__ n_dev, SweepChain chain) {
     constexpr int NW = kSortThreads / 32;
     constexpr uint32_t TILE = kSortThreads * ROWS;
     static_assert(ROWS % 4 == 0, "the ranking takes four rows at a time");
+    static_assert(kSortThreads == (int)kRadix, "one thread per digit");
     constexpr uint32_t FULL = 0xffffffffu;
     __shared__ uint32_t s_keys[TILE];
     __shared__ uint32_t s_vals[TILE];
@@ -280,6 +273,8 @@ __global__ __launch_bounds__(kSortThreads, 4) void k_onesweep(const uint32_t* __
             *chain.my_dirty = tiles * kRadix;
         }
     }
+    // this pass's digit offsets: the exclusive scan of its digit counts (thread d: digit d)
+    const uint32_t digit_base = block_exclusive_scan<kSortThreads>(digit_count[tid], s_warp, nullptr);
   for (;;) {  // a block takes tiles until none is left (the grid may be smaller than the tiles)
     __syncthreads();  // the previous tile's shared memory is free
     if (tid == 0) s_tile = atomicAdd(ticket, 1u);
@@ -383,7 +378,7 @@ __global__ __launch_bounds__(kSortThreads, 4) void k_onesweep(const uint32_t* __
         }
         st_relaxed(my_lb, kFlagPrefix | ((excl + tot) & kValueMask));
     }
-    s_global_base[d] = digit_offset[d] + excl;
+    s_global_base[d] = digit_base + excl;
     const uint32_t local_start = block_exclusive_scan<kSortThreads>(tot, s_warp, nullptr);
     s_local_start[d] = local_start;
     __syncthreads();  // every thread reads other digits' starts below
@@ -656,13 +651,8 @@ cudaError_t launch_step(cudaStream_t s, const StepLaunch& a) {
     return cudaGetLastError();
 }
 
-cudaError_t launch_hist_scan(cudaStream_t s, const uint32_t* hist, uint32_t* offsets, uint32_t passes) {
-    k_hist_scan<<<1, kRadix, 0, s>>>(hist, offsets, passes);
-    return cudaGetLastError();
-}
-
 cudaError_t launch_onesweep(cudaStream_t s, const uint32_t* keys_in, const uint32_t* vals_in, uint32_t* keys_out,
-                            uint32_t* vals_out, uint32_t n, uint32_t shift, const uint32_t* digit_offset,
+                            uint32_t* vals_out, uint32_t n, uint32_t shift, const uint32_t* digit_count,
                             uint32_t* lookback, uint32_t* ticket, uint32_t* err, const uint32_t* n_dev,
                             const SweepChain* chain) {
     if (n == 0) return cudaSuccess;
@@ -683,11 +673,11 @@ cudaError_t launch_onesweep(cudaStream_t s, const uint32_t* keys_in, const uint3
         const unsigned grid =
             std::min<unsigned>(blocks_for(n, kSortThreads * kSortRowsDev), 4u * (unsigned)(sms > 0 ? sms : 1));
         k_onesweep<true, kSortRowsDev><<<grid, kSortThreads, 0, s>>>(keys_in, vals_in, keys_out, vals_out, n, shift,
-                                                                     digit_offset, lookback, ticket, err, n_dev, ch);
+                                                                     digit_count, lookback, ticket, err, n_dev, ch);
         return cudaGetLastError();
     }
     k_onesweep<false, kSortRows><<<blocks_for(n, kSortTile), kSortThreads, 0, s>>>(
-        keys_in, vals_in, keys_out, vals_out, n, shift, digit_offset, lookback, ticket, err, n_dev, ch);
+        keys_in, vals_in, keys_out, vals_out, n, shift, digit_count, lookback, ticket, err, n_dev, ch);
     return cudaGetLastError();
 }
 

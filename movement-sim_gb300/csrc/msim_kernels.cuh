@@ -55,7 +55,6 @@ cudaError_t launch_init_entities(cudaStream_t s, const DeviceMap& m, EntityState
                                  uint32_t rng_kind, uint64_t seed, uint32_t placement, float smin,
                                  float smax);
 cudaError_t launch_step(cudaStream_t s, const StepLaunch& a);
-cudaError_t launch_hist_scan(cudaStream_t s, const uint32_t* hist, uint32_t* offsets, uint32_t passes);
 // Look-back bookkeeping that lets consecutive radix passes run without a memset
 // between them: before its tiles a pass zeroes next_lookback[0, *next_dirty) and
 // *next_ticket, and sets *my_dirty to the look-back words it publishes itself.  The
@@ -70,7 +69,7 @@ struct SweepChain {
 size_t sort_lookback_words(uint32_t n);
 cudaError_t launch_onesweep(cudaStream_t s, const uint32_t* keys_in, const uint32_t* vals_in,
                             uint32_t* keys_out, uint32_t* vals_out, uint32_t n, uint32_t shift,
-                            const uint32_t* digit_offset, uint32_t* lookback, uint32_t* ticket,
+                            const uint32_t* digit_count, uint32_t* lookback, uint32_t* ticket,
                             uint32_t* err, const uint32_t* n_dev = nullptr,  // n_dev: count on the device (<= n)
                             const SweepChain* chain = nullptr);
 cudaError_t launch_ranges(cudaStream_t s, const uint32_t* sorted_key, uint32_t n, uint2* ranges, uint32_t num_keys,

@@ -42,8 +42,7 @@ constexpr size_t kOffSv0 = kOffSk0 + kMaxN;
 constexpr size_t kOffSk1 = kOffSv0 + kMaxN;
 constexpr size_t kOffSv1 = kOffSk1 + kMaxN;
 constexpr size_t kOffHist = kOffSv1 + kMaxN;
-constexpr size_t kOffDigit = kOffHist + kMaxPasses * kRadix;
-constexpr size_t kOffTickets = kOffDigit + kMaxPasses * kRadix;
+constexpr size_t kOffTickets = kOffHist + kMaxPasses * kRadix;
 constexpr size_t kOffStatus = kOffTickets + 64;
 constexpr size_t kOffLookback = kOffStatus + 64;
 constexpr size_t kOffRanges = kOffLookback + (size_t)kMaxPasses * kMaxSortTiles * kRadix;
@@ -209,7 +208,6 @@ extern "C" int msim_query_neighbours_noalloc(const float* d_pos, uint32_t n, flo
 
     bool ok = cudaMemsetAsync(w + kOffHist, 0, sizeof(uint32_t) * kMaxPasses * kRadix, s) == cudaSuccess;
     ok = ok && launch_step(s, a) == cudaSuccess;
-    ok = ok && launch_hist_scan(s, w + kOffHist, w + kOffDigit, passes) == cudaSuccess;
     ok = ok && cudaMemsetAsync(w + kOffLookback, 0, sizeof(uint32_t) * (size_t)passes * sort_tiles * kRadix, s) == cudaSuccess;
     ok = ok && cudaMemsetAsync(w + kOffTickets, 0, sizeof(uint32_t) * kMaxPasses, s) == cudaSuccess;
     uint32_t* sk[2] = {w + kOffSk0, w + kOffSk1};
@@ -217,7 +215,7 @@ extern "C" int msim_query_neighbours_noalloc(const float* d_pos, uint32_t n, flo
     for (uint32_t ps = 0; ok && ps < passes; ps++) {
         const uint32_t* kin = ps == 0 ? w + kOffKey : sk[(ps - 1) & 1];
         const uint32_t* vin = ps == 0 ? nullptr : sv[(ps - 1) & 1];
-        ok = launch_onesweep(s, kin, vin, sk[ps & 1], sv[ps & 1], n, 8u * ps, w + kOffDigit + ps * kRadix,
+        ok = launch_onesweep(s, kin, vin, sk[ps & 1], sv[ps & 1], n, 8u * ps, w + kOffHist + ps * kRadix,
                              w + kOffLookback + (size_t)ps * sort_tiles * kRadix, w + kOffTickets + ps,
                              status) == cudaSuccess;
     }
