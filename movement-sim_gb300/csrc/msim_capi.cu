@@ -98,6 +98,7 @@ struct msim_ctx {
     uint32_t* ab_counts = nullptr;
     unsigned long long* mark_lookback = nullptr;
     uint32_t* mark_ticket = nullptr;
+    size_t update_words = 0;  // hist, mark ticket and mark look-back lie together: one memset per update
     uint32_t* merge_split = nullptr;
     // entries that went through the radix passes since the stats were reset: full
     // sorts counted on the host, incremental updates' changed entries on the device
@@ -422,10 +423,19 @@ int build_index(msim_ctx* c) {
 
 // One tick of the move plus the index, from the previous sorted order: split it by
 // whether each key changed, sort the changed entries, merge (writing the key-start
-// table and the sorted positions on the way).
+// table and the sorted positions on the way).  The update's scratch (digit counts,
+// split ticket and look-back words) is cleared first, in one memset, before the
+// move, so that the move step and the split run back to back.
 int incremental_update(msim_ctx* c);
 
+int clear_update_scratch(msim_ctx* c) {
+    CK(cudaMemsetAsync(c->hist, 0, sizeof(uint32_t) * c->update_words, c->stream), "memset update scratch");
+    return MSIM_OK;
+}
+
 int incremental_index(msim_ctx* c) {
+    int rc = clear_update_scratch(c);
+    if (rc != MSIM_OK) return rc;
     {
         Prof p(c, K_STEP);
         StepLaunch a = step_args(c, 1, true);
@@ -437,7 +447,6 @@ int incremental_index(msim_ctx* c) {
 
 // The update itself, for new keys (by slot) already in c->key.
 int incremental_update(msim_ctx* c) {
-    CK(cudaMemsetAsync(c->hist, 0, sizeof(uint32_t) * kMaxPasses * kRadix, c->stream), "memset hist");
     {
         Prof p(c, K_MARK);
         CK(launch_mark(c->stream, c->sorted_slot, c->order_identity, c->sorted_key, c->key, c->n, c->passes,
@@ -682,13 +691,14 @@ int msim_create(const msim_map* map, const msim_params* params, msim_ctx** out) 
             (rc = dalloc(c, &c->st[b].slot_id, n)) || (rc = dalloc(c, &c->sk[b], n)) || (rc = dalloc(c, &c->sv[b], n)))
             return bail(rc);
     }
-    if ((rc = dalloc(c, &c->key, n)) || (rc = dalloc(c, &c->hist, (size_t)kMaxPasses * kRadix)) ||
+    // [digit counts | split ticket, pad | split look-back words (8-byte aligned)]
+    c->update_words = (size_t)kMaxPasses * kRadix + 2u + 2u * (size_t)mark_tiles(c->n);
+    if ((rc = dalloc(c, &c->key, n)) || (rc = dalloc(c, &c->hist, c->update_words)) ||
         (rc = dalloc(c, &c->lookback, (size_t)kMaxPasses * c->sort_region)) ||
         (rc = dalloc(c, &c->sort_dirty, (size_t)kMaxPasses)) ||
         (rc = dalloc(c, &c->tickets, (size_t)kMaxPasses)) || (rc = dalloc(c, &c->a_key, n)) || (rc = dalloc(c, &c->a_val, n)) ||
         (rc = dalloc(c, &c->b_key[0], n)) || (rc = dalloc(c, &c->b_key[1], n)) || (rc = dalloc(c, &c->b_val[0], n)) ||
         (rc = dalloc(c, &c->b_val[1], n)) || (rc = dalloc(c, &c->ab_counts, 2)) ||
-        (rc = dalloc(c, &c->mark_lookback, mark_tiles(c->n))) || (rc = dalloc(c, &c->mark_ticket, 1)) ||
         (rc = dalloc(c, &c->merge_split, (size_t)merge_tiles(c->n) + 1)) || (rc = dalloc(c, &c->sorted_dev, 1)) ||
         (rc = dalloc(c, &c->nbr_count, n)) || (rc = dalloc(c, &c->pairs, kPairBins)) || (rc = dalloc(c, &c->err, 1)) ||
         (rc = dalloc(c, &c->check, 1)))
@@ -699,6 +709,8 @@ int msim_create(const msim_map* map, const msim_params* params, msim_ctx** out) 
             (rc = dalloc(c, &c->kstart_chunk_count_b[b], 1)) || (rc = dalloc(c, &c->sorted_pos_b[b], n)))
             return bail(rc);
     }
+    c->mark_ticket = c->hist + (size_t)kMaxPasses * kRadix;
+    c->mark_lookback = reinterpret_cast<unsigned long long*>(c->hist + (size_t)kMaxPasses * kRadix + 2u);
     use_index_buffers(c, 0);
     if (p.cap > 0) {
         size_t blocks = (n + kQueryThreads - 1) / kQueryThreads;
@@ -948,6 +960,7 @@ int msim_tick_host(msim_ctx* c, const float* in_pos, const uint32_t* in_heading,
     const bool in_place = dev_head != nullptr;
     CK(cudaMemsetAsync(c->check, 0xff, sizeof(uint32_t), c->stream), "memset check");
     if (nbr && !use_inc) CK(cudaMemsetAsync(c->hist, 0, sizeof(uint32_t) * kMaxPasses * kRadix, c->stream), "memset hist");
+    if (use_inc && (rc = clear_update_scratch(c)) != MSIM_OK) return rc;
     CK(cudaEventRecord(c->ev_start, c->stream), "cudaEventRecord");
     CK(cudaStreamWaitEvent(c->up, c->ev_start, 0), "cudaStreamWaitEvent");
 

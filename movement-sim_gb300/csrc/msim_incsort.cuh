@@ -57,6 +57,7 @@ __global__ __launch_bounds__(kMarkThreads, 5) void k_mark(const uint32_t* __rest
     __shared__ uint32_t s_bal[kMarkPer * NW];                // the (row, warp) ballots of unchanged keys
     __shared__ uint32_t s_tile, s_pa, s_pb;
     const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    chain_enter();
     if (tid == 0) s_tile = atomicAdd(ticket, 1u);
     for (uint32_t i = tid; i < passes * kRadix; i += kMarkThreads) s_hist[i] = 0u;
     __syncthreads();
@@ -197,6 +198,7 @@ __global__ __launch_bounds__(256) void k_merge_path(const uint32_t* __restrict__
                                                     const uint32_t* __restrict__ counts, uint32_t n,
                                                     uint32_t boundaries, uint32_t* __restrict__ split) {
     constexpr uint32_t FULL = 0xffffffffu;
+    chain_enter();
     const uint32_t t = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const uint32_t lane = threadIdx.x & 31;
     if (t >= boundaries) return;  // uniform per warp
@@ -238,6 +240,7 @@ __global__ __launch_bounds__(kMergeThreads) void k_merge(
     __shared__ uint32_t s_ink[kMergeTile], s_inv[kMergeTile];    // A segment, then B segment
     __shared__ uint32_t s_outk[kMergeTile], s_outv[kMergeTile];
     __shared__ uint32_t s_prev;  // clamped key of the entry before the tile
+    chain_enter();
     const uint32_t tid = threadIdx.x, lane = tid & 31;
     const uint32_t na_all = counts[0], nb_all = counts[1];
     if (na_all + nb_all != n) {  // unreachable unless the split look-back gave up

@@ -32,6 +32,18 @@ constexpr uint32_t kValueMask = 0x3fffffffu;
 constexpr uint32_t kSpinLimit = 1u << 24;  // ~1 s of polling, then give up with kErrTimeout
 constexpr int kLookBack = 4;               // predecessor tiles read per look-back round of a radix pass
 
+// Kernels of the per-tick chain (move, split, radix passes, merge, key-start fill,
+// re-ordering) are launched with programmatic stream serialisation: a chain kernel
+// lets the next one launch once all its own blocks run, and waits for its
+// predecessor to finish, with its writes visible, before it touches global memory.
+// Only the launch and block dispatch overlap the predecessor's tail.  A dependent is
+// launched only when every block of its predecessor is resident, so waiting blocks
+// never keep a predecessor's block from being scheduled.
+__device__ __forceinline__ void chain_enter() {
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+}
+
 __device__ __forceinline__ uint32_t lanemask_lt() {
     uint32_t m;
     asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
@@ -150,11 +162,12 @@ template <int RNG, bool KEY>
 __global__ __launch_bounds__(kStepThreads) void k_step(StepLaunch a) {
     __shared__ uint32_t s_hist[kMaxPasses * kRadix];
     __shared__ uint32_t s_morton[KEY ? 2048 : 1];
-    if (KEY) {
+    if (KEY) {  // shared memory only: overlaps the predecessor's tail
         for (uint32_t i = threadIdx.x; i < a.passes * kRadix; i += kStepThreads) s_hist[i] = 0u;
         for (uint32_t i = threadIdx.x; i < 2048u; i += kStepThreads) s_morton[i] = part1by1(i);
         __syncthreads();
     }
+    chain_enter();
     const uint32_t lane = threadIdx.x & 31;
     const uint32_t stride = gridDim.x * kStepThreads;
     for (uint32_t base = blockIdx.x * kStepThreads; base < a.n; base += 2u * stride) {
@@ -262,6 +275,7 @@ __global__ __launch_bounds__(kSortThreads, 4) void k_onesweep(const uint32_t* __
     __shared__ uint32_t s_tile;
 
     const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    chain_enter();
     if (n_dev) n = min(*n_dev, n);  // item count known only on the device (grid sized for n)
     const uint32_t tiles = n ? (n + TILE - 1u) / TILE : 1u;
     if (chain.next_lookback) {  // clear the next pass's look-back words and ticket
@@ -496,6 +510,7 @@ __device__ __noinline__ void list_overflow(const uint32_t* __restrict__ sorted_s
 #include "msim_incsort.cuh"
 
 __global__ void k_permute(const uint32_t* __restrict__ ss, EntityState src, EntityState dst, uint32_t n) {
+    chain_enter();
     const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= n) return;
     const uint32_t s = ss[p] < n ? ss[p] : p;
@@ -612,6 +627,22 @@ __global__ void k_iota(uint32_t* out, uint32_t n) {
 
 inline unsigned blocks_for(uint32_t n, unsigned threads) { return (unsigned)((n + threads - 1) / threads); }
 
+// Launch of a chain kernel (see chain_enter).
+template <typename... KArgs, typename... Args>
+cudaError_t launch_chained(void (*kernel)(KArgs...), unsigned grid, unsigned block, cudaStream_t s, Args... args) {
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(block);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = s;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kernel, static_cast<KArgs>(args)...);
+}
+
 }  // namespace
 
 
@@ -642,11 +673,11 @@ cudaError_t launch_step(cudaStream_t s, const StepLaunch& a) {
     if (a.n == 0) return cudaSuccess;
     const bool key = a.key != nullptr;
     if (a.rng_kind == 1) {
-        if (key) k_step<1, true><<<a.blocks, kStepThreads, 0, s>>>(a);
-        else k_step<1, false><<<a.blocks, kStepThreads, 0, s>>>(a);
+        return key ? launch_chained(k_step<1, true>, a.blocks, kStepThreads, s, a)
+                   : launch_chained(k_step<1, false>, a.blocks, kStepThreads, s, a);
     } else {
-        if (key) k_step<0, true><<<a.blocks, kStepThreads, 0, s>>>(a);
-        else k_step<0, false><<<a.blocks, kStepThreads, 0, s>>>(a);
+        return key ? launch_chained(k_step<0, true>, a.blocks, kStepThreads, s, a)
+                   : launch_chained(k_step<0, false>, a.blocks, kStepThreads, s, a);
     }
     return cudaGetLastError();
 }
@@ -672,13 +703,11 @@ cudaError_t launch_onesweep(cudaStream_t s, const uint32_t* keys_in, const uint3
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         const unsigned grid =
             std::min<unsigned>(blocks_for(n, kSortThreads * kSortRowsDev), 4u * (unsigned)(sms > 0 ? sms : 1));
-        k_onesweep<true, kSortRowsDev><<<grid, kSortThreads, 0, s>>>(keys_in, vals_in, keys_out, vals_out, n, shift,
-                                                                     digit_count, lookback, ticket, err, n_dev, ch);
-        return cudaGetLastError();
+        return launch_chained(k_onesweep<true, kSortRowsDev>, grid, kSortThreads, s, keys_in, vals_in, keys_out,
+                              vals_out, n, shift, digit_count, lookback, ticket, err, n_dev, ch);
     }
-    k_onesweep<false, kSortRows><<<blocks_for(n, kSortTile), kSortThreads, 0, s>>>(
-        keys_in, vals_in, keys_out, vals_out, n, shift, digit_count, lookback, ticket, err, n_dev, ch);
-    return cudaGetLastError();
+    return launch_chained(k_onesweep<false, kSortRows>, blocks_for(n, kSortTile), kSortThreads, s, keys_in, vals_in,
+                          keys_out, vals_out, n, shift, digit_count, lookback, ticket, err, n_dev, ch);
 }
 
 size_t sort_lookback_words(uint32_t n) {
@@ -715,14 +744,14 @@ cudaError_t launch_kstart(cudaStream_t s, const uint32_t* sorted_key, uint32_t n
         const uint32_t cap = kstart_chunk_cap(num_keys);
         cudaError_t e = cudaMemsetAsync(chunk_count, 0, sizeof(uint32_t), s);
         if (e != cudaSuccess) return e;
-        k_kstart_pos<<<blocks_for(n + 1u, 256), 256, 0, s>>>(sorted_key, n, kstart, num_keys, chunks, chunk_count,
-                                                             cap, sorted_slot, pos, sorted_pos);
-        e = cudaGetLastError();
+        e = launch_chained(k_kstart_pos, blocks_for(n + 1u, 256), 256, s, sorted_key, n, kstart, num_keys, chunks,
+                           chunk_count, cap, sorted_slot, pos, sorted_pos);
         if (e != cudaSuccess) return e;
         int dev = 0, sms = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        k_kstart_fill<<<4 * (sms > 0 ? sms : 1), 256, 0, s>>>(chunks, chunk_count, cap, kstart);
+        e = launch_chained(k_kstart_fill, 4u * (sms > 0 ? sms : 1), 256, s, chunks, chunk_count, cap, kstart);
+        if (e != cudaSuccess) return e;
         if (kernels) *kernels = 2;
     } else {
         const uint64_t warps = (entries + kKstartWindow - 1u) / kKstartWindow;
@@ -786,12 +815,8 @@ cudaError_t launch_mark(cudaStream_t s, const uint32_t* P, bool identity, const 
                         uint32_t* counts, uint32_t* err, unsigned long long* changed_total) {
     if (n == 0) return cudaMemsetAsync(counts, 0, 2 * sizeof(uint32_t), s);
     const uint32_t tiles = mark_tiles(n);
-    cudaError_t e = cudaMemsetAsync(lookback, 0, sizeof(unsigned long long) * tiles, s);
-    if (e == cudaSuccess) e = cudaMemsetAsync(ticket, 0, sizeof(uint32_t), s);
-    if (e != cudaSuccess) return e;
-    k_mark<<<tiles, kMarkThreads, 0, s>>>(P, identity ? 1u : 0u, PK, NK, n, passes, a_key, a_val, b_key, b_val, hist,
-                                          lookback, ticket, tiles, counts, err, changed_total);
-    return cudaGetLastError();
+    return launch_chained(k_mark, tiles, kMarkThreads, s, P, identity ? 1u : 0u, PK, NK, n, passes, a_key, a_val, b_key,
+                          b_val, hist, lookback, ticket, tiles, counts, err, changed_total);
 }
 
 cudaError_t launch_merge(cudaStream_t s, const uint32_t* a_key, const uint32_t* a_val, const uint32_t* b_key,
@@ -803,20 +828,19 @@ cudaError_t launch_merge(cudaStream_t s, const uint32_t* a_key, const uint32_t* 
     if (n == 0 || num_keys == 0) return cudaSuccess;
     const uint32_t tiles = merge_tiles(n);
     const uint32_t cap = kstart_chunk_cap(num_keys);
-    k_merge_path<<<(tiles + 1u + 7u) / 8u, 256, 0, s>>>(a_key, b_key, counts, n, tiles + 1u, split);  // a warp each
-    cudaError_t e = cudaGetLastError();
-    if (e == cudaSuccess) e = cudaMemsetAsync(chunk_count, 0, sizeof(uint32_t), s);
-    if (e != cudaSuccess) return e;
-    k_merge<<<tiles, kMergeThreads, 0, s>>>(a_key, a_val, b_key, b_val, counts, split, n, out_key, out_val, pos,
-                                            sorted_pos, kstart, num_keys, chunks, chunk_count, cap, err);
-    e = cudaGetLastError();
+    cudaError_t e = cudaMemsetAsync(chunk_count, 0, sizeof(uint32_t), s);  // first: the three kernels chain
+    if (e == cudaSuccess)  // a warp per tile boundary
+        e = launch_chained(k_merge_path, (tiles + 1u + 7u) / 8u, 256, s, a_key, b_key, counts, n, tiles + 1u, split);
+    if (e == cudaSuccess)
+        e = launch_chained(k_merge, tiles, kMergeThreads, s, a_key, a_val, b_key, b_val, counts, split, n, out_key,
+                           out_val, pos, sorted_pos, kstart, num_keys, chunks, chunk_count, cap, err);
     if (e != cudaSuccess) return e;
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    k_kstart_fill<<<4 * (sms > 0 ? sms : 1), 256, 0, s>>>(chunks, chunk_count, cap, kstart);
-    if (kernels) *kernels = 3;
-    return cudaGetLastError();
+    e = launch_chained(k_kstart_fill, 4u * (sms > 0 ? sms : 1), 256, s, chunks, chunk_count, cap, kstart);
+    if (e == cudaSuccess && kernels) *kernels = 3;
+    return e;
 }
 
 cudaError_t launch_iota(cudaStream_t s, uint32_t* out, uint32_t n) {
@@ -827,8 +851,7 @@ cudaError_t launch_iota(cudaStream_t s, uint32_t* out, uint32_t n) {
 
 cudaError_t launch_permute(cudaStream_t s, const uint32_t* sorted_slot, EntityState src, EntityState dst, uint32_t n) {
     if (n == 0) return cudaSuccess;
-    k_permute<<<blocks_for(n, 256), 256, 0, s>>>(sorted_slot, src, dst, n);
-    return cudaGetLastError();
+    return launch_chained(k_permute, blocks_for(n, 256), 256, s, sorted_slot, src, dst, n);
 }
 
 cudaError_t launch_export_state(cudaStream_t s, EntityState st, uint32_t n, float2* pos, uint32_t* head, uint4* rng,

@@ -92,6 +92,7 @@ cudaError_t launch_query(cudaStream_t s, uint32_t cap, const uint32_t* kstart, c
 // -> counts[0..1]; B's digit counts -> hist), then, after B is sorted, merge A and B
 // into out_key / out_val, writing the key-start table and the sorted positions.
 // changed_total (may be NULL) accumulates |B| (entries that go through the sort).
+// lookback (mark_tiles(n) words), ticket and hist must be zero when the split starts.
 uint32_t mark_tiles(uint32_t n);
 uint32_t merge_tiles(uint32_t n);
 cudaError_t launch_mark(cudaStream_t s, const uint32_t* P, bool identity, const uint32_t* PK, const uint32_t* NK,

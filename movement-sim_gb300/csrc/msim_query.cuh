@@ -158,6 +158,7 @@ __global__ __launch_bounds__(256) void k_kstart_pos(const uint32_t* __restrict__
                                                     uint4* __restrict__ chunks, uint32_t* chunk_count,
                                                     uint32_t chunk_cap, const uint32_t* __restrict__ sv,
                                                     const float2* __restrict__ pos, float2* __restrict__ sorted_pos) {
+    chain_enter();
     const uint32_t lane = threadIdx.x & 31;
     const uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
     if (sorted_pos && q < n) {  // positions in sorted order, for the query's candidate reads
@@ -176,6 +177,7 @@ __global__ __launch_bounds__(256) void k_kstart_pos(const uint32_t* __restrict__
 __global__ __launch_bounds__(256) void k_kstart_fill(const uint4* __restrict__ chunks,
                                                      const uint32_t* __restrict__ chunk_count, uint32_t chunk_cap,
                                                      uint32_t* __restrict__ kstart) {
+    chain_enter();
     const uint32_t lane = threadIdx.x & 31;
     const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
     const uint32_t count = min(*chunk_count, chunk_cap);
