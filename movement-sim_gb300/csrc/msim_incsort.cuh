@@ -106,7 +106,14 @@ __global__ __launch_bounds__(kMarkThreads, 5) void k_mark(const uint32_t* __rest
             s_off[lane * E + k] = run;
             run += v[k];
         }
-        if (lane == 31) s_off[kMarkPer * NW] = run;
+        if (lane == 31) {
+            s_off[kMarkPer * NW] = run;
+            // publish the tile's counts at once: later tiles' look-back need not wait
+            // for this tile's staging
+            const uint32_t ta = run, tb = (n > base ? min(n - base, kMarkTile) : 0u) - run;
+            st_relaxed64(lookback + tile,
+                         (tile == 0 ? kMarkPrefix : kMarkAgg) | ((unsigned long long)ta << 31) | tb);
+        }
     }
     __syncthreads();
     const uint32_t valid_in_tile = n > base ? min(n - base, kMarkTile) : 0u;
@@ -127,9 +134,7 @@ __global__ __launch_bounds__(kMarkThreads, 5) void k_mark(const uint32_t* __rest
             for (uint32_t ps = 0; ps < passes; ps++)
                 atomicAdd(&s_hist[ps * kRadix + ((kn[r] >> (8u * ps)) & 0xffu)], 1u);
     }
-    if (warp == 0) {  // publish and look back
-        const unsigned long long agg = ((unsigned long long)tot_a << 31) | tot_b;
-        if (lane == 0) st_relaxed64(lookback + tile, (tile == 0 ? kMarkPrefix : kMarkAgg) | agg);
+    if (warp == 0) {  // look back (the counts were published after the scan)
         uint32_t ea = 0u, eb = 0u;
         if (tile > 0) {
             int32_t j = (int32_t)tile - 1;
