@@ -236,7 +236,9 @@ __global__ __launch_bounds__(256) void k_merge_path(const uint32_t* __restrict__
 // entries, in shared memory (ranks by binary search in the other segment), then
 // writes the sorted keys and slots, the positions in sorted order and the key-start
 // entries owned by each position (fill_key_gaps).
-__global__ __launch_bounds__(kMergeThreads) void k_merge(
+// 8 blocks per SM (32 registers): 0.158 ms at 16 M against 0.173 at the 40 registers
+// the compiler picks alone (6 blocks).
+__global__ __launch_bounds__(kMergeThreads, 8) void k_merge(
     const uint32_t* __restrict__ a_key, const uint32_t* __restrict__ a_val, const uint32_t* __restrict__ b_key,
     const uint32_t* __restrict__ b_val, const uint32_t* __restrict__ counts, const uint32_t* __restrict__ split,
     uint32_t n, uint32_t* __restrict__ out_key, uint32_t* __restrict__ out_val, const float2* __restrict__ pos,
@@ -273,13 +275,30 @@ __global__ __launch_bounds__(kMergeThreads) void k_merge(
         }
         s_prev = prev;
     }
-    for (uint32_t i = tid; i < na; i += kMergeThreads) {
-        s_ink[i] = a_key[a0 + i];
-        s_inv[i] = a_val[a0 + i];
-    }
-    for (uint32_t i = tid; i < nb; i += kMergeThreads) {
-        s_ink[na + i] = b_key[b0 + i];
-        s_inv[na + i] = b_val[b0 + i];
+    constexpr uint32_t kPer = kMergeTile / kMergeThreads;
+    {  // every load of a thread is in flight before the first shared store
+        uint32_t ik[kPer], iv[kPer];
+#pragma unroll
+        for (uint32_t k = 0; k < kPer; k++) {
+            const uint32_t i = k * kMergeThreads + tid;
+            ik[k] = 0u;
+            iv[k] = 0u;
+            if (i < na) {
+                ik[k] = a_key[a0 + i];
+                iv[k] = a_val[a0 + i];
+            } else if (i < na + nb) {
+                ik[k] = b_key[b0 + (i - na)];
+                iv[k] = b_val[b0 + (i - na)];
+            }
+        }
+#pragma unroll
+        for (uint32_t k = 0; k < kPer; k++) {
+            const uint32_t i = k * kMergeThreads + tid;
+            if (i < na + nb) {
+                s_ink[i] = ik[k];
+                s_inv[i] = iv[k];
+            }
+        }
     }
     __syncthreads();
     for (uint32_t i = tid; i < na + nb; i += kMergeThreads) {
@@ -310,8 +329,16 @@ __global__ __launch_bounds__(kMergeThreads) void k_merge(
     __syncthreads();
     const uint32_t cnt = d1 - d0;
     const uint32_t prev_tile = s_prev;
-    for (uint32_t i0 = 0; i0 < kMergeTile; i0 += kMergeThreads) {
-        const uint32_t i = i0 + tid;
+    float2 gp[kPer];  // the positions of a thread's outputs, gathered together
+#pragma unroll
+    for (uint32_t k = 0; k < kPer; k++) {
+        const uint32_t i = k * kMergeThreads + tid;
+        const uint32_t slot = i < cnt ? s_outv[i] : n;
+        gp[k] = slot < n ? pos[slot] : make_float2(__int_as_float(0x7fffffff), __int_as_float(0x7fffffff));
+    }
+#pragma unroll
+    for (uint32_t k = 0; k < kPer; k++) {
+        const uint32_t i = k * kMergeThreads + tid;
         const bool ok = i < cnt;
         uint32_t from = 0, len = 0;
         const uint32_t p = d0 + i;
@@ -319,7 +346,7 @@ __global__ __launch_bounds__(kMergeThreads) void k_merge(
             const uint32_t key = s_outk[i], slot = s_outv[i];
             out_key[p] = key;
             out_val[p] = slot;
-            sorted_pos[p] = slot < n ? pos[slot] : make_float2(__int_as_float(0x7fffffff), __int_as_float(0x7fffffff));
+            sorted_pos[p] = gp[k];
             const uint32_t kc = key < num_keys ? key : num_keys - 1u;
             uint32_t kp = i > 0 ? s_outk[i - 1u] : prev_tile;
             if (i > 0) kp = kp < num_keys ? kp : num_keys - 1u;
