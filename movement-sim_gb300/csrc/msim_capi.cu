@@ -538,7 +538,9 @@ int run_query(msim_ctx* c, bool overlap) {
     CK(cudaMemsetAsync(c->pairs, 0, sizeof(unsigned long long) * kPairBins, qs), "memset pairs");
     {
         Prof p(c, K_QUERY);
-        CK(launch_query(qs, c->params.cap, c->kstart, c->sorted_slot, c->sorted_pos, cur_state(c).slot_id, c->grid,
+        // slots that hold their own entity need no id lookup
+        CK(launch_query(qs, c->params.cap, c->kstart, c->sorted_slot, c->sorted_pos,
+                        c->slots_identity ? nullptr : cur_state(c).slot_id, c->grid,
                         c->n, c->nbr_count, c->nbr_list, c->pairs),
            "k_query");
     }
@@ -961,6 +963,9 @@ int msim_tick_host(msim_ctx* c, const float* in_pos, const uint32_t* in_heading,
     CK(cudaMemsetAsync(c->check, 0xff, sizeof(uint32_t), c->stream), "memset check");
     if (nbr && !use_inc) CK(cudaMemsetAsync(c->hist, 0, sizeof(uint32_t) * kMaxPasses * kRadix, c->stream), "memset hist");
     if (use_inc && (rc = clear_update_scratch(c)) != MSIM_OK) return rc;
+    // entity i in slot i (for later calls; this tick's query and export take the slot
+    // as the id): written first, beside the first chunk's upload
+    CK(launch_iota(c->stream, s.slot_id, n), "k_iota");
     CK(cudaEventRecord(c->ev_start, c->stream), "cudaEventRecord");
     CK(cudaStreamWaitEvent(c->up, c->ev_start, 0), "cudaStreamWaitEvent");
 
@@ -1015,7 +1020,6 @@ int msim_tick_host(msim_ctx* c, const float* in_pos, const uint32_t* in_heading,
                                c->down),
                "download rng");
     }
-    CK(launch_iota(c->stream, s.slot_id, n), "k_iota");  // entity i in slot i
     c->cur = b;
     c->slots_identity = true;
     if (use_inc) {
@@ -1035,7 +1039,7 @@ int msim_tick_host(msim_ctx* c, const float* in_pos, const uint32_t* in_heading,
             uint32_t* d_idx = want_idx ? d_count + n : nullptr;
             {
                 Prof p(c, K_EXPORT);
-                CK(launch_export_neighbours(c->stream, c->sorted_slot, s.slot_id, c->nbr_count, c->nbr_list, n,
+                CK(launch_export_neighbours(c->stream, c->sorted_slot, nullptr, c->nbr_count, c->nbr_list, n,
                                             c->params.cap, d_count, d_idx),
                    "k_export_nbr");
             }

@@ -493,7 +493,7 @@ __device__ __noinline__ void list_overflow(const uint32_t* __restrict__ sorted_s
                 if (q == p || !in_range(sorted_pos[q], me, g.radius)) continue;
                 const uint32_t s2 = sorted_slot[q];
                 if (s2 >= n) continue;
-                const uint32_t oid = slot_id[s2];
+                const uint32_t oid = slot_id ? slot_id[s2] : s2;
                 if (m == cap && oid >= out[cap - 1]) continue;
                 uint32_t j = m < cap ? m++ : cap - 1;
                 while (j > 0 && out[j - 1] > oid) {
@@ -550,7 +550,7 @@ __global__ __launch_bounds__(kQueryThreads) void k_export_nbr(const uint32_t* so
     if (p >= n) return;
     const uint32_t s = sorted_slot ? sorted_slot[p] : p;
     if (s >= n) return;
-    const uint32_t id = slot_id[s];
+    const uint32_t id = slot_id ? slot_id[s] : s;  // NULL: slot s holds entity s
     if (id >= n) return;
     out_count[id] = c;
     if (out_idx && cap) {

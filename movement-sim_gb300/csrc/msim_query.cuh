@@ -444,7 +444,7 @@ __global__ __launch_bounds__(kQueryThreads, 16) void k_query(const uint32_t* __r
                 id[i] = 0xffffffffu;
                 if ((uint32_t)i < wmax) {
                     const uint32_t s2 = (uint32_t)i < count ? sorted_slot[sh.keep[i][tid]] : n;
-                    id[i] = s2 < n ? slot_id[s2] : 0xffffffffu;
+                    id[i] = s2 < n ? (slot_id ? slot_id[s2] : s2) : 0xffffffffu;  // NULL: slot = id
                 }
             }
             uint32_t keep[kRegKeep];  // ascending; unused slots hold 0xffffffff
