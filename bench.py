@@ -73,7 +73,7 @@ KERNEL_BYTES = {
 # one ncu capture of the same workload at full size (third neighbour tick; 1-pass
 # metrics; profiles/scale_16M_dram_traffic.md); scaled by the entities of the run
 NCU_DRAM_BYTES_PER_ENTITY = {
-    "scale": {"k_query": 26.83, "k_merge": 32.60, "k_mark": 16.90, "k_step": 28.14},
+    "scale": {"k_query": 26.87, "k_merge": 32.78, "k_mark": 16.91, "k_step": 27.98},
     "neighbours": {"k_query": 24.07, "k_onesweep": 6.91},
 }
 
