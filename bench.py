@@ -251,7 +251,10 @@ def run_ours(args, cfg, world, rank, local):
         kernels[name] = {"launches": v["launches"], "avg_ms": avg, "share": v["ms"] / total_ms,
                          "algo_bytes_per_launch": per_launch_bytes,
                          "achieved_gbs": per_launch_bytes / (avg / 1e3) / 1e9 if avg > 0 else None}
-    dominant = max(kernels.items(), key=lambda kv: kv[1]["share"])
+    # the dominant kernel: the largest time of one launch per tick (a radix pass is one
+    # of three launches per tick; the re-ordering runs once in many ticks), the unit
+    # the roofline's achieved figure is taken over
+    dominant = max(kernels.items(), key=lambda kv: kv[1]["avg_ms"] * min(1.0, kv[1]["launches"] / prof_steps))
     traffic = None
     per_entity = NCU_DRAM_BYTES_PER_ENTITY.get(args.config, {}).get(dominant[0])
     if per_entity is not None and not any(getattr(args, k) is not None for k in ("entities", "lattice", "cap")):

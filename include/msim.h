@@ -128,9 +128,9 @@ typedef struct msim_params {
 
 /* msim_params.flags: how neighbour ticks rebuild the index (same results either way).
  * By default the previous order is updated (only entries whose key changed are
- * sorted and merged back) from 4,000,000 entities on, and fully re-sorted below.
+ * sorted and merged back; the first neighbour tick sorts fully).
  * FULL_SORT: always a full radix sort (e.g. entities that move far between ticks);
- * INCREMENTAL: always the update. */
+ * INCREMENTAL: the update (the default; kept for callers that name it). */
 #define MSIM_PARAM_FULL_SORT 1u
 #define MSIM_PARAM_INCREMENTAL 2u
 

@@ -608,9 +608,10 @@ int msim_create(const msim_map* map, const msim_params* params, msim_ctx** out) 
         return cuda_fail(e, "cudaGetDevice");
     }
     c->params = p;
-    // the incremental index update pays off from a few million entities on
-    c->incremental = (p.flags & MSIM_PARAM_FULL_SORT) == 0 &&
-                     ((p.flags & MSIM_PARAM_INCREMENTAL) != 0 || p.num_entities >= 4000000u);
+    // the incremental index update is the faster one at every size measured (62.5 K,
+    // 250 K, 1 M and 16 M entities at the lattice density: 0.051 against 0.060 ms per
+    // tick at 62.5 K, 0.092 against 0.114 at 1 M)
+    c->incremental = (p.flags & MSIM_PARAM_FULL_SORT) == 0;
     c->n = p.num_entities;
     c->R = map->num_roads;
     c->C = map->num_connections;
