@@ -69,6 +69,7 @@ struct msim_ctx {
     uint32_t* lookback = nullptr;   // kMaxPasses regions of sort_region words, chained (see sweep_chain)
     uint32_t* tickets = nullptr;
     uint32_t* sort_dirty = nullptr; // per region: look-back words its last pass published
+    bool chain_broken = false;      // a pass failed to launch: the regions' state is unknown
     size_t sort_region = 0;
     // The index the query reads (current buffer set).  Two sets, paired with the two
     // sorted-slot buffers: a tick's merge writes the set the previous tick's query does
@@ -343,10 +344,15 @@ SweepChain sweep_chain(msim_ctx* c, uint32_t ps) {
     return ch;
 }
 
+// Also after a pass failed to launch (a later pass then did not clear the region the
+// next sort starts with): every region, ticket and extent is zeroed again.
 int clear_unchained(msim_ctx* c) {
-    if (c->passes >= 2) return MSIM_OK;
-    CK(cudaMemsetAsync(c->lookback, 0, sizeof(uint32_t) * c->sort_region, c->stream), "memset lookback");
+    if (c->passes >= 2 && !c->chain_broken) return MSIM_OK;
+    const size_t words = c->chain_broken ? kMaxPasses * c->sort_region : c->sort_region;
+    CK(cudaMemsetAsync(c->lookback, 0, sizeof(uint32_t) * words, c->stream), "memset lookback");
     CK(cudaMemsetAsync(c->tickets, 0, sizeof(uint32_t) * kMaxPasses, c->stream), "memset tickets");
+    CK(cudaMemsetAsync(c->sort_dirty, 0, sizeof(uint32_t) * kMaxPasses, c->stream), "memset look-back extents");
+    c->chain_broken = false;
     return MSIM_OK;
 }
 
@@ -368,6 +374,7 @@ int sort_keys(msim_ctx* c) {
     if (rc != MSIM_OK) return rc;
     rc = join_query(c);  // the passes rewrite the sorted slots the last query reads
     if (rc != MSIM_OK) return rc;
+    c->chain_broken = true;  // until every pass has launched
     for (uint32_t ps = 0; ps < c->passes; ps++) {
         const uint32_t* kin = ps == 0 ? c->key : c->sk[(ps - 1) & 1];
         const uint32_t* vin = ps == 0 ? nullptr : c->sv[(ps - 1) & 1];
@@ -378,6 +385,7 @@ int sort_keys(msim_ctx* c) {
                            nullptr, c->passes >= 2 ? &ch : nullptr),
            "k_onesweep");
     }
+    c->chain_broken = false;
     c->sorted_key = c->sk[(c->passes - 1) & 1];
     c->sorted_slot = c->sv[(c->passes - 1) & 1];
     c->have_sort = true;
@@ -457,6 +465,7 @@ int incremental_update(msim_ctx* c) {
     }
     int rc = clear_unchained(c);
     if (rc != MSIM_OK) return rc;
+    c->chain_broken = true;  // until every pass has launched
     for (uint32_t ps = 0; ps < c->passes; ps++) {  // stable radix sort of the changed entries
         const SweepChain ch = sweep_chain(c, ps);
         Prof p(c, K_SORT_PASS);
@@ -466,6 +475,7 @@ int incremental_update(msim_ctx* c) {
                            c->passes >= 2 ? &ch : nullptr),
            "k_onesweep");
     }
+    c->chain_broken = false;
     // The merge writes the sorted slots and index buffer set the previous tick's query
     // does not read (that query may still run); it waits for the query before that.
     const int out = c->sorted_key == c->sk[0] ? 1 : 0;
