@@ -11,10 +11,10 @@
 //   k_kstart    key-start table: first sorted position of every key (tile + band)
 //   k_query     radius neighbour query (random_move.comp:541-719 semantics: the
 //               pair predicate of :551-562), count + the cap smallest ids
-// From 4 M entities the sort is replaced by an incremental update of the previous
-// order (msim_incsort.cuh): k_mark splits it by changed keys, k_onesweep sorts the
-// changed entries, k_merge_path + k_merge merge them back and write the key-start
-// table and the sorted positions.
+// After the first neighbour tick the sort is replaced by an incremental update of the
+// previous order (msim_incsort.cuh): k_mark splits it by changed keys, k_onesweep
+// sorts the changed entries, k_merge_path + k_merge merge them back and write the
+// key-start table and the sorted positions.
 // Every few ticks k_permute re-orders the entity state by the sorted order so
 // that the step and the query keep reading memory almost sequentially.
 #include <algorithm>
