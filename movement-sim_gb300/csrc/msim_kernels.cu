@@ -263,7 +263,8 @@ __global__ __launch_bounds__(kSortThreads, 4) void k_onesweep(const uint32_t* __
                                                               const uint32_t* __restrict__ n_dev, SweepChain chain) {
     constexpr int NW = kSortThreads / 32;
     constexpr uint32_t TILE = kSortThreads * ROWS;
-    static_assert(ROWS % 4 == 0, "the ranking takes four rows at a time");
+    constexpr int G = ROWS < 4 ? ROWS : 4;  // rows whose counter atomics are in flight together
+    static_assert(ROWS % G == 0, "whole groups of rows");
     static_assert(kSortThreads == (int)kRadix, "one thread per digit");
     constexpr uint32_t FULL = 0xffffffffu;
     __shared__ uint32_t s_keys[TILE];
@@ -323,10 +324,10 @@ __global__ __launch_bounds__(kSortThreads, 4) void k_onesweep(const uint32_t* __
     // (2) leaders take their group's counts, in row order, four rows in flight;
     // (3) broadcast from the leaders
 #pragma unroll
-    for (int r0 = 0; r0 < ROWS; r0 += 4) {
-        uint32_t old[4];
+    for (int r0 = 0; r0 < ROWS; r0 += G) {
+        uint32_t old[G];
 #pragma unroll
-        for (int q = 0; q < 4; q++) {
+        for (int q = 0; q < G; q++) {
             const int r = r0 + q;
             old[q] = 0u;
             const uint32_t idx = row0 + r * 32;
@@ -334,7 +335,7 @@ __global__ __launch_bounds__(kSortThreads, 4) void k_onesweep(const uint32_t* __
                 old[q] = atomicAdd(&wh[(k[r] >> shift) & 0xffu], rk[r] >> 16);
         }
 #pragma unroll
-        for (int q = 0; q < 4; q++) {
+        for (int q = 0; q < G; q++) {
             const int r = r0 + q;
             const uint32_t from_leader = __shfl_sync(FULL, old[q], (rk[r] >> 8) & 0x1fu);
             rk[r] = from_leader + (rk[r] & 0xffu);
