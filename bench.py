@@ -20,6 +20,7 @@ import json
 import os
 import subprocess
 import sys
+import tempfile
 import time
 from pathlib import Path
 
@@ -55,7 +56,8 @@ def b_nbr(k_mean: float) -> float:
     return 36.0 + 4.0 * k_mean
 
 
-# per-kernel algorithmic bytes per entity and launch
+# per-kernel algorithmic bytes per entity and launch: the per-entity figures of a
+# neighbour tick (24 B move + 36 + 4 k B index and query) split over the kernels
 KERNEL_BYTES = {
     "k_step": lambda k: B_STEP + 4,        # move + key write
     "k_onesweep": lambda k: 16,            # (key, id) read + write
@@ -72,6 +74,10 @@ KERNEL_BYTES = {
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per entity and launch of
 # one ncu capture of the same workload at full size (third neighbour tick; 1-pass
 # metrics; profiles/scale_16M_dram_traffic.md); scaled by the entities of the run
+# warp instructions per entity-step of k_batch_step (smsp__inst_executed.sum of one
+# ncu capture over entities x ticks of the launch); None until captured
+NCU_BATCH_WARP_INSTR_PER_ENTITY_STEP = None
+
 NCU_DRAM_BYTES_PER_ENTITY = {
     "scale": {"k_query": 26.87, "k_merge": 32.78, "k_mark": 16.91, "k_step": 27.98},
     "neighbours": {"k_query": 24.07, "k_onesweep": 6.91},
@@ -137,7 +143,7 @@ class ClockSampler:
     def __init__(self, gpu_index: int):
         self.gpu = gpu_index
         self.proc = None
-        self.path = ROOT / "gpurun_out" / f"clocks_{os.getpid()}.csv"
+        self.path = Path(tempfile.gettempdir()) / f"msim_clocks_{os.getpid()}_{gpu_index}.csv"
 
     def __enter__(self):
         try:
@@ -164,7 +170,9 @@ class ClockSampler:
         if not self.proc or not self.path.exists():
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
         rows = []
-        for line in self.path.read_text().splitlines():
+        text = self.path.read_text()
+        self.path.unlink(missing_ok=True)
+        for line in text.splitlines():
             parts = [x.strip() for x in line.split(",")]
             if len(parts) < 9:
                 continue
@@ -217,6 +225,15 @@ def run_ours(args, cfg, world, rank, local):
     launches = sim.launch_count() - launches0
     ms_max = max_over_ranks(ms, world)
     value = world * n * args.steps / (ms_max / 1e3)
+    # the workload's full tick count in one timed region (includes the re-orderings
+    # of the state that a short window may miss)
+    barrier_sync(world)
+    sim.timer_begin()
+    tick(cfg["ticks"])
+    ms_cfg = max_over_ranks(sim.timer_end(), world)
+    sim.sync()
+    config_run = {"ticks": cfg["ticks"], "ms_per_step": ms_cfg / cfg["ticks"],
+                  "value": world * n * cfg["ticks"] / (ms_cfg / 1e3), "unit": "entity-steps/s"}
 
     # mean kept neighbours of the last tick
     k_mean = 0.0
@@ -276,11 +293,11 @@ def run_ours(args, cfg, world, rank, local):
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
-        cpu = cpu_baseline(cfg, road_map, budget_s=args.cpu_budget)
+        cpu = cpu_baseline(cfg, budget_s=args.cpu_budget)
     return {
         "value": value, "ms_per_step": ms_max / args.steps, "clocks": clocks.summary(), "k_mean": k_mean,
         "roofline": roofline, "roofline_tick": roofline_tick, "kernels": kernels, "e2e": e2e, "cpu": cpu,
-        "launches": launches, "info": info, "roads": road_map.num_roads,
+        "launches": launches, "info": info, "roads": road_map.num_roads, "config_run": config_run,
         "sorted_fraction": sorted_per_update / max(n, 1),
     }
 
@@ -351,13 +368,13 @@ def run_batched(args, world, rank, local):
     log-uniform 1e3..2e5, seed = index + SEED) advanced `steps` ticks by one
     persistent graph-captured launch, against one-at-a-time plain launches."""
     pkg = importlib.import_module("movement-sim_gb300")
-    sides, ents, seeds = pkg.ensemble_config(args.instances, SEED)
+    sides, ents, seeds = ensemble_config(args.instances, SEED)
     maps = [pkg.RoadMap.lattice(s, sd) for s, sd in zip(sides, seeds)]
     total = sum(ents)
     batch = pkg.Batch(maps, ents, rng="pcg32", dt=DT)
     batch.init_entities(seeds, placement="fraction", speed=SPEED)
     t_tune = time.perf_counter()
-    batch.tune(min(args.steps, 100), ROOT / "gpurun_out" / "batch_tune_cache.txt" if args.tune_cache else None)
+    batch.tune(min(args.steps, 100), args.tune_cache)
     t_tune = time.perf_counter() - t_tune
     batch.init_entities(seeds, placement="fraction", speed=SPEED)
     batch.step(args.steps)  # warm-up: builds the graph for this tick count
@@ -399,14 +416,51 @@ def run_batched(args, world, rank, local):
     # speed 4, rng rarely): the HBM bytes of the launch
     launch_bytes = total * 28
     gbs = launch_bytes / (ms / 1e3) / 1e9
-    return {"value": value, "ms_per_step": ms_max / args.steps, "clocks": clocks.summary(), "launches": launches,
+    clk = clocks.summary()
+    # The kernel keeps every entity's state in registers for all ticks of the launch,
+    # so it is bound by instruction issue, not HBM: achieved = warp instructions per
+    # entity-step (from an ncu capture of the kernel) x entity-steps/s, against one
+    # warp instruction per cycle on each of the 4 schedulers of the 152 SMs.
+    sm_mhz = clk.get("sm_mhz") or 2070.0
+    issue_peak = 152 * 4 * sm_mhz * 1e6
+    ipe = NCU_BATCH_WARP_INSTR_PER_ENTITY_STEP
+    issue = None
+    if ipe is not None:
+        ach = ipe * value / world
+        issue = {"bound": "issue", "kernel": "k_batch_step", "achieved": ach, "peak": issue_peak,
+                 "unit": "warp-instructions/s", "frac": round(ach / issue_peak, 4),
+                 "warp_instructions_per_entity_step": ipe, "sm_mhz": sm_mhz}
+    return {"value": value, "ms_per_step": ms_max / args.steps, "clocks": clk, "launches": launches,
             "one_at_a_time": {"value": one_value, "unit": "entity-steps/s", "seconds": one_s,
                               "what": "each instance alone (msim_step without neighbours), synchronised one by one"},
             "speedup_vs_one_at_a_time": value / one_value, "schedule": sched, "tune_seconds": t_tune,
-            "instances": len(maps), "total_entities": total,
+            "instances": len(maps), "total_entities": total, "issue": issue,
             "roofline": {"bound": "hbm", "kernel": "k_batch_step", "achieved": round(gbs, 1), "peak": peak,
                          "unit": "GB/s", "frac": round(gbs / peak, 4), "traffic": None, "peak_source": peak_kind,
-                         "note": "state stays in registers for all ticks of a launch: 28 B per entity per launch"}}
+                         "note": "not the bound: the state stays in registers for all ticks of a launch (28 B "
+                                 "per entity per launch); see issue"}}
+
+
+def run_forms(args, world, rank, local):
+    """Short runs of the two other forms, added to the default line: the batched
+    ensemble (512 instances, 1,000 ticks in one launch, against one-at-a-time
+    launches) and the calibration step (forward + adjoint, 2 steps after 1 warm-up)."""
+    a = argparse.Namespace(**vars(args))
+    a.steps, a.warmup, a.no_e2e, a.no_cpu, a.ticks = CONFIGS["batched"]["ticks"], 3, True, True, None
+    b = run_batched(a, world, rank, local)
+    a.steps, a.warmup = 2, 1
+    d = run_adjoint(a, world, rank, local)
+    return {"batched": {"workload": "512 instances, lattice side U{16..256}, entities log-U[1e3, 2e5], "
+                                    f"{b['total_entities']} entities, 1,000 ticks in one launch",
+                        "value": b["value"], "unit": "entity-steps/s", "ms_per_tick": b["ms_per_step"],
+                        "one_at_a_time": b["one_at_a_time"]["value"],
+                        "speedup_vs_one_at_a_time": b["speedup_vs_one_at_a_time"], "issue": b["issue"],
+                        "schedule": b["schedule"]},
+            "adjoint": {"workload": "262,144 entities, 128x128 lattice, 2,000 ticks, 512x512 grid, K = 100",
+                        "value": d["value"], "unit": "entity-steps/s (forward + backward entity-ticks)",
+                        "ms_per_step": d["ms_per_step"], "forward_ms": d["forward_ms"],
+                        "backward_ms": d["backward_ms"], "step_over_forward": d["step_over_forward"],
+                        "roofline": d["roofline"]}}
 
 
 def run_adjoint(args, world, rank, local):
@@ -495,7 +549,9 @@ def run_adjoint(args, world, rank, local):
     calib.close()
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
-        cpu = cpu_adjoint(rm, T, budget_entities=args.cpu_entities)
+        from oracle import oracle as orc
+
+        cpu = cpu_adjoint(orc, orc.lattice(cfg["lattice"], SEED), args.cpu_entities or n, T, orc.cpu_count())
     return {"value": value, "ms_per_step": ms_max / args.steps, "clocks": clocks.summary(), "roofline": roofline,
             "kernels": kern, "phases_ms": ph, "forward_ms": fwd_ms, "backward_ms": bwd_ms,
             "backward_over_forward": bwd_ms / fwd_ms, "step_over_forward": (fwd_ms + bwd_ms) / fwd_ms,
@@ -503,13 +559,9 @@ def run_adjoint(args, world, rank, local):
             "launches": args.steps * (3 + S + 3 + 3 + 2)}
 
 
-def cpu_adjoint(rm, ticks, budget_entities=65536):
-    """The FP64 CPU adjoint (forward, loss, reverse sweep) on a bounded sample of the
-    calibration workload: budget_entities entities over all ticks, host threads."""
-    from oracle import oracle as orc
-
-    threads = orc.cpu_count()
-    n = budget_entities
+def cpu_adjoint(orc, rm, n, ticks, threads):
+    """The FP64 CPU adjoint (forward, loss, reverse sweep) of the calibration
+    workload: n entities over all ticks, host threads."""
     pos, head, rng, speed = orc.init_entities(rm.road_pos, n, 1, SEED, 1, SPEED[0], SPEED[1])
     state = {"pos": pos, "heading": head, "rng": rng}
     target = np.zeros(ADJ_GRID[0] * ADJ_GRID[1], np.float32)
@@ -522,107 +574,117 @@ def cpu_adjoint(rm, ticks, budget_entities=65536):
                       f"and reverse sweep), {threads} threads"}
 
 
-def oracle_tick_loop(orc, road_map, state, cfg, ticks, threads):
-    pos, head, rng, speed = state
-    if not cfg["neighbours"]:  # entities are independent: every thread runs all ticks on its range
-        orc.step(road_map.road_pos, road_map.road_conn, road_map.connections, pos, head, rng, speed, 1, DT, ticks,
-                 threads=threads)
-        return
-    for _ in range(ticks):
-        orc.step(road_map.road_pos, road_map.road_conn, road_map.connections, pos, head, rng, speed, 1, DT, 1,
-                 threads=threads)
-        if cfg["neighbours"]:
-            orc.neighbours(pos, cfg["radius"], cfg["cap"], threads=threads, with_idx=True)
+def ensemble_config(count: int = 512, seed: int = SEED, side_range=(16, 256), entity_range=(1_000, 200_000)):
+    """Instance sizes of the batched ensemble: lattice side uniform in side_range
+    (inclusive), entity count log-uniform in entity_range, instance seed = index +
+    seed; numpy's PCG64 generator seeded by `seed`.  (The package's ensemble_config
+    gives the same lists; a CPU test checks it.)"""
+    rs = np.random.default_rng(seed)
+    sides = rs.integers(side_range[0], side_range[1] + 1, count)
+    lo, hi = np.log(entity_range[0]), np.log(entity_range[1])
+    entities = np.floor(np.exp(rs.uniform(lo, hi, count))).astype(np.int64)
+    seeds = np.arange(count, dtype=np.int64) + seed
+    return [int(x) for x in sides], [int(x) for x in entities], [int(x) for x in seeds]
 
 
-def cpu_sample_config(cfg):
-    """A bounded sample of the workload for the host cores: at most 2M entities at the
-    workload's density (entities per road), on a correspondingly smaller lattice."""
-    if cfg["entities"] <= 2_000_000:
-        return dict(cfg), "full workload"
-    scale = cfg["entities"] // 2_000_000
-    side = int(round(cfg["lattice"] / np.sqrt(scale)))
-    s = dict(cfg, lattice=side, entities=cfg["entities"] // scale)
-    return s, f"{s['entities']} entities on a {side}x{side} lattice (same entities per road as the workload)"
+class OracleWorkload:
+    """A workload on the host cores with the oracle C restatement, built from the
+    oracle's own lattice generator (nothing of the product is loaded): the entities
+    of the workload, and per tick the move step and, for neighbour workloads, the
+    CPU-grid query with the id lists, into arrays reused across ticks."""
+
+    def __init__(self, orc, lattice: int, n: int, cfg: dict, threads: int, seed: int = SEED):
+        self.orc, self.cfg, self.threads, self.n = orc, cfg, threads, n
+        self.rm = orc.lattice(lattice, seed)
+        self.state = orc.init_entities(self.rm.road_pos, n, 1, seed, 1, SPEED[0], SPEED[1])
+        self.nbr = bool(cfg["neighbours"])
+        if self.nbr:
+            self.out = (np.empty(n, np.uint32), np.empty((n, cfg["cap"]), np.uint32) if cfg["cap"] else None)
+
+    def ticks(self, ticks: int) -> None:
+        orc, rm = self.orc, self.rm
+        pos, head, rng, speed = self.state
+        if not self.nbr:  # independent entities: every thread runs all ticks on its range
+            orc.step(rm.road_pos, rm.road_conn, rm.connections, pos, head, rng, speed, 1, DT, ticks,
+                     threads=self.threads)
+            return
+        for _ in range(ticks):
+            orc.step(rm.road_pos, rm.road_conn, rm.connections, pos, head, rng, speed, 1, DT, 1, threads=self.threads)
+            orc.neighbours(pos, self.cfg["radius"], self.cfg["cap"], threads=self.threads, with_idx=True,
+                           out=self.out)
+
+    def what(self) -> str:
+        return ("oracle C restatement of random_move.comp (move" +
+                (" + CPU-grid neighbour query with id lists)" if self.nbr else " only)"))
 
 
-def cpu_baseline(cfg, road_map, budget_s=20.0, kind="port"):
+def cpu_baseline(cfg, budget_s=20.0):
+    """The oracle on the full workload (same map, entities and seed as the GPU run),
+    timed on the host cores for whole ticks until about budget_s seconds."""
     from oracle import oracle as orc
 
     threads = orc.cpu_count()
-    sample, desc = cpu_sample_config(cfg)
-    pkg = importlib.import_module("movement-sim_gb300")
-    rm = road_map if sample["lattice"] == cfg["lattice"] else pkg.RoadMap.lattice(sample["lattice"], SEED)
-    n = sample["entities"]
-    state = orc.init_entities(rm.road_pos, n, 1, SEED, 1, SPEED[0], SPEED[1])
-    oracle_tick_loop(orc, rm, state, sample, 1, threads)  # warm-up tick
+    w = OracleWorkload(orc, cfg["lattice"], cfg["entities"], cfg, threads)
+    w.ticks(1)  # warm-up tick
     ticks = 0
     t0 = time.perf_counter()
     while True:
-        oracle_tick_loop(orc, rm, state, sample, 1, threads)
+        w.ticks(1)
         ticks += 1
         el = time.perf_counter() - t0
-        if el > budget_s or ticks >= (sample["ticks"]):
+        if el > budget_s or ticks >= cfg["ticks"]:
             break
-    return {"value": n * ticks / el, "unit": "entity-steps/s", "cores": threads, "kind": kind,
-            "sample": f"{ticks} ticks of {desc}: oracle C restatement ("
-                      f"{'move + CPU-grid neighbour query' if sample['neighbours'] else 'move only'}), "
-                      f"{threads} threads"}
+    return {"value": cfg["entities"] * ticks / el, "unit": "entity-steps/s", "cores": threads, "kind": "port",
+            "sample": f"{ticks} ticks (after 1 warm-up tick) of the full workload ({cfg['entities']} entities, "
+                      f"{cfg['lattice']}x{cfg['lattice']} lattice): {w.what()}, {threads} threads"}
 
 
 def run_reference(args, cfg, world, rank):
-    """The reference's CPU path restated (the Vulkan shader needs a graphics stack that
-    neither machine has), timed on the host cores: each step is one tick over a
-    bounded sample of the workload."""
+    """The reference's path on the host cores (the Vulkan shader needs a graphics
+    stack that neither machine has, so it is the oracle C restatement of the shader,
+    with the same threading as shader_validation): W warm-up steps, then K timed
+    steps of the same workload as the GPU arm.  Loads only oracle/ libraries."""
     if rank != 0:
         return None
     from oracle import oracle as orc
 
-    pkg = importlib.import_module("movement-sim_gb300")
     threads = orc.cpu_count()
-    if args.config == "adjoint":  # each step: the FP64 calibration step on a bounded sample
-        rm = pkg.RoadMap.lattice(cfg["lattice"], SEED)
+    if args.config == "adjoint":  # each step: the FP64 calibration step (forward, loss, reverse sweep)
+        n = args.cpu_entities or cfg["entities"]
+        rm = orc.lattice(cfg["lattice"], SEED)
         for _ in range(min(args.warmup, 1)):
-            cpu_adjoint(rm, cfg["ticks"], args.cpu_entities)
+            cpu_adjoint(orc, rm, n, cfg["ticks"], threads)
         t0 = time.perf_counter()
         for _ in range(args.steps):
-            r = cpu_adjoint(rm, cfg["ticks"], args.cpu_entities)
+            r = cpu_adjoint(orc, rm, n, cfg["ticks"], threads)
         el = time.perf_counter() - t0
-        v = args.cpu_entities * cfg["ticks"] * args.steps / el
-        return {"value": v, "ms_per_step": el * 1e3 / args.steps, "threads": threads, "sample": r["sample"],
-                "sample_line": f"each step {r['sample']}"}
-    if args.config == "batched":  # each step: one tick of the first instances (>= 1M entities)
-        sides, ents, seeds = pkg.ensemble_config(args.instances, SEED)
-        chosen, total = [], 0
-        for side, n_i, sd in zip(sides, ents, seeds):
-            if total >= 1_000_000:
-                break
-            rm = pkg.RoadMap.lattice(side, sd)
-            chosen.append((rm, orc.init_entities(rm.road_pos, n_i, 1, sd, 1, SPEED[0], SPEED[1])))
-            total += n_i
+        return {"value": n * cfg["ticks"] * args.steps / el, "ms_per_step": el * 1e3 / args.steps,
+                "threads": threads, "sample": f"each step {r['sample']}"}
+    if args.config == "batched":  # each step: one move tick of every instance
+        sides, ents, seeds = ensemble_config(args.instances, SEED)
         move = dict(neighbours=False)
+        inst = [OracleWorkload(orc, side, n_i, move, threads, seed=sd) for side, n_i, sd in zip(sides, ents, seeds)]
+        total = sum(ents)
 
         def run(ticks):
-            for rm, state in chosen:
-                oracle_tick_loop(orc, rm, state, move, ticks, threads)
+            for w in inst:
+                w.ticks(ticks)
 
         run(args.warmup)
         t0 = time.perf_counter()
         run(args.steps)
         el = time.perf_counter() - t0
-        desc = f"the first {len(chosen)} ensemble instances ({total} entities), move only"
         return {"value": total * args.steps / el, "ms_per_step": el * 1e3 / args.steps, "threads": threads,
-                "sample": desc, "sample_line": f"each step one tick of {desc}; oracle C restatement of the move step"}
-    sample, desc = cpu_sample_config(cfg)
-    rm = pkg.RoadMap.lattice(sample["lattice"], SEED)
-    n = sample["entities"]
-    state = orc.init_entities(rm.road_pos, n, 1, SEED, 1, SPEED[0], SPEED[1])
-    oracle_tick_loop(orc, rm, state, sample, args.warmup, threads)
+                "sample": f"each step one move tick of all {len(inst)} ensemble instances ({total} entities), "
+                          f"instance after instance; oracle C restatement of the move step, {threads} threads"}
+    w = OracleWorkload(orc, cfg["lattice"], cfg["entities"], cfg, threads)
+    w.ticks(args.warmup)
     t0 = time.perf_counter()
-    oracle_tick_loop(orc, rm, state, sample, args.steps, threads)
+    w.ticks(args.steps)
     el = time.perf_counter() - t0
-    v = n * args.steps / el
-    return {"value": v, "ms_per_step": el * 1e3 / args.steps, "threads": threads, "sample": desc}
+    return {"value": cfg["entities"] * args.steps / el, "ms_per_step": el * 1e3 / args.steps, "threads": threads,
+            "sample": f"each step one tick of the full workload ({cfg['entities']} entities, "
+                      f"{cfg['lattice']}x{cfg['lattice']} lattice): {w.what()}, {threads} threads"}
 
 
 def main():
@@ -634,6 +696,8 @@ def main():
     ap.add_argument("--config", choices=sorted(CONFIGS), default="scale")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-forms", action="store_true",
+                    help="scale config: skip the short batched and adjoint runs added to the line")
     ap.add_argument("--e2e-steps", type=int, default=10)
     ap.add_argument("--cpu-budget", type=float, default=15.0)
     ap.add_argument("--entities", type=int, default=None, help="override (profiling runs)")
@@ -641,8 +705,9 @@ def main():
     ap.add_argument("--cap", type=int, default=None, help="override (profiling runs)")
     ap.add_argument("--ticks", type=int, default=None, help="adjoint config: ticks per step (profiling runs)")
     ap.add_argument("--instances", type=int, default=512, help="batched config: number of instances")
-    ap.add_argument("--tune-cache", action="store_true", help="batched config: reuse/append the tuner cache")
-    ap.add_argument("--cpu-entities", type=int, default=65536, help="adjoint config: CPU baseline sample size")
+    ap.add_argument("--tune-cache", default=None, help="batched config: tuner cache file to reuse/append")
+    ap.add_argument("--cpu-entities", type=int, default=None,
+                    help="adjoint config: entities of the CPU adjoint (default: the workload's)")
     args = ap.parse_args()
     cfg = dict(CONFIGS[args.config])
     for k in ("entities", "lattice", "cap", "ticks"):
@@ -651,8 +716,71 @@ def main():
     if args.steps is None:
         args.steps = 5 if args.config == "adjoint" else cfg["ticks"]
     args.warmup = max(args.warmup, 3)
-    world, rank, local = dist_setup(args)
+    if args.impl == "reference":  # host cores only: no process group, rank 0 alone runs
+        world, rank, local = int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("RANK", "0")), 0
+    else:
+        world, rank, local = dist_setup(args)
+    config = workload_config(args, cfg, world)
+    line = {"metric": "entity-steps/s", "unit": "entity-steps/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded lattice road graph and entities)", "config": config}
 
+    if args.impl == "reference":
+        r = run_reference(args, cfg, world, rank)
+        if rank == 0:
+            line.update({"impl": "reference", "value": r["value"], "ms_per_step": r["ms_per_step"],
+                         "cpu_baseline": {"value": r["value"], "unit": "entity-steps/s", "cores": r["threads"],
+                                          "kind": "port",
+                                          "sample": r["sample"] + "; the Vulkan shader itself is unavailable on "
+                                                                  "this box (no graphics stack)"},
+                         "e2e": {"value": r["value"], "unit": "entity-steps/s", "h2d_bytes_per_step": 0,
+                                 "d2h_bytes_per_step": 0}})
+            print(json.dumps(line), flush=True)
+        return
+
+    if args.config == "batched":
+        r = run_batched(args, world, rank, local)
+        if rank == 0:
+            line.update({k: r[k] for k in ("value", "ms_per_step", "clocks", "roofline", "one_at_a_time",
+                                            "speedup_vs_one_at_a_time", "issue")})
+            line.update({"schedule": r["schedule"], "tune_seconds": round(r["tune_seconds"], 2),
+                         "gpu_launches": r["launches"], "cpu_baseline": None, "e2e": None})
+            print(json.dumps(line), flush=True)
+        return
+    if args.config == "adjoint":
+        r = run_adjoint(args, world, rank, local)
+        if rank == 0:
+            line.update({k: r[k] for k in ("value", "ms_per_step", "clocks", "roofline", "e2e")})
+            line.update({"cpu_baseline": r["cpu"], "gpu_launches": r["launches"], "kernels": r["kernels"],
+                         "roads": r["roads"], "phases_ms": r["phases_ms"], "forward_ms": r["forward_ms"],
+                         "backward_ms": r["backward_ms"], "backward_over_forward": r["backward_over_forward"],
+                         "step_over_forward": r["step_over_forward"], "loss": r["loss"]})
+            print(json.dumps(line), flush=True)
+        return
+    r = run_ours(args, cfg, world, rank, local)
+    forms = None
+    if args.config == "scale" and not args.no_forms and not any(getattr(args, k) is not None
+                                                                 for k in ("entities", "lattice", "cap")):
+        forms = run_forms(args, world, rank, local)
+    if rank == 0:
+        line.update({"value": r["value"], "ms_per_step": r["ms_per_step"], "roofline": r["roofline"],
+                     "roofline_tick": r["roofline_tick"], "cpu_baseline": r["cpu"], "e2e": r["e2e"],
+                     "clocks": r["clocks"], "gpu_launches": r["launches"], "config_length_run": r["config_run"],
+                     "index": {"roads": r["roads"], "tiles": [r["info"]["tiles_x"], r["info"]["tiles_y"]],
+                               "cell_m": round(r["info"]["cell_size"], 3), "sort_passes": r["info"]["sort_passes"],
+                               "resort_interval": r["info"]["resort_interval"],
+                               "mean_kept_neighbours": round(r["k_mean"], 4),
+                               "sorted_fraction_per_tick": round(r["sorted_fraction"], 5)},
+                     "kernels": {k: {kk: (round(vv, 5) if isinstance(vv, float) else vv) for kk, vv in v.items()}
+                                 for k, v in r["kernels"].items()}})
+        if forms is not None:
+            line["forms"] = forms
+        print(json.dumps(line), flush=True)
+
+
+def workload_config(args, cfg, world):
+    """The workload as both arms print it (nothing measured: the same dict for the
+    GPU arm and the reference arm)."""
     workload = {
         "scale": "plain+neighbours at scale: 16,000,000 entities, 1024x1024 lattice, radius 2.0 m, cap 64",
         "neighbours": "plain+neighbours: 1,000,000 entities, 256x256 lattice, radius 2.0 m, cap 64",
@@ -670,70 +798,15 @@ def main():
               "parallelism": f"replicas x{world}",
               "l2": "inputs larger than L2 (entity state 32 B x entities)" if cfg["entities"] * 32 > 129e6
               else "working set fits in L2 (small config)"}
-    line = {"metric": "entity-steps/s", "unit": "entity-steps/s", "n_gpus": world, "steps": args.steps,
-            "warmup": args.warmup, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-            "data": "synthetic (seeded lattice road graph and entities)", "config": config}
-
-    if args.impl == "reference":
-        r = run_reference(args, cfg, world, rank)
-        if rank == 0:
-            line.update({"impl": "reference", "value": r["value"], "ms_per_step": r["ms_per_step"],
-                         "cpu_baseline": {"value": r["value"], "unit": "entity-steps/s", "cores": r["threads"],
-                                          "kind": "port",
-                                          "sample": r.get("sample_line") or
-                                          f"each step one tick of {r['sample']}; oracle C restatement "
-                                          "of random_move.comp (the Vulkan shader itself is unavailable "
-                                          "on this box: no graphics stack)"},
-                         "e2e": {"value": r["value"], "unit": "entity-steps/s", "h2d_bytes_per_step": 0,
-                                 "d2h_bytes_per_step": 0}})
-            config["parallelism"] = "host cores"
-            print(json.dumps(line), flush=True)
-        return
-
     if args.config == "batched":
-        r = run_batched(args, world, rank, local)
-        if rank == 0:
-            config.update({"instances": r["instances"], "entities": r["total_entities"], "lattice": "U{16..256}",
-                           "schedule": r["schedule"], "tune_seconds": round(r["tune_seconds"], 2),
-                           "l2": "inputs larger than L2 (28 B x total entities per launch)"})
-            line.update({k: r[k] for k in ("value", "ms_per_step", "clocks", "roofline", "one_at_a_time",
-                                            "speedup_vs_one_at_a_time")})
-            line["gpu_launches"] = r["launches"]
-            line["cpu_baseline"] = None
-            line["e2e"] = None
-            print(json.dumps(line), flush=True)
-        return
+        _, ents, _ = ensemble_config(args.instances, SEED)
+        config.update({"instances": args.instances, "entities": sum(ents), "lattice": "U{16..256}",
+                       "l2": "inputs larger than L2 (28 B x total entities per launch)"})
     if args.config == "adjoint":
-        if args.impl == "reference":
-            return
-        r = run_adjoint(args, world, rank, local)
-        if rank == 0:
-            config.update({"roads": r["roads"], "ticks_per_step": cfg["ticks"], "grid": list(ADJ_GRID),
-                           "checkpoint_interval": ADJ_K, "hidden_factors": "U[0.7, 1.3] from the seed",
-                           "l2": "inputs larger than L2 (checkpoints and per-segment history)"})
-            line.update({k: r[k] for k in ("value", "ms_per_step", "clocks", "roofline", "e2e")})
-            line.update({"cpu_baseline": r["cpu"], "gpu_launches": r["launches"], "kernels": r["kernels"],
-                         "phases_ms": r["phases_ms"], "forward_ms": r["forward_ms"], "backward_ms": r["backward_ms"],
-                         "backward_over_forward": r["backward_over_forward"],
-                         "step_over_forward": r["step_over_forward"], "loss": r["loss"]})
-            print(json.dumps(line), flush=True)
-        return
-    r = run_ours(args, cfg, world, rank, local)
-    if rank == 0:
-        config["roads"] = r["roads"]
-        config["tiles"] = [r["info"]["tiles_x"], r["info"]["tiles_y"]]
-        config["cell_m"] = round(r["info"]["cell_size"], 3)
-        config["sort_passes"] = r["info"]["sort_passes"]
-        config["resort_interval"] = r["info"]["resort_interval"]
-        config["mean_kept_neighbours"] = round(r["k_mean"], 4)
-        config["sorted_fraction_per_tick"] = round(r["sorted_fraction"], 5)
-        line.update({"value": r["value"], "ms_per_step": r["ms_per_step"], "roofline": r["roofline"],
-                     "roofline_tick": r["roofline_tick"], "cpu_baseline": r["cpu"], "e2e": r["e2e"],
-                     "clocks": r["clocks"], "gpu_launches": r["launches"],
-                     "kernels": {k: {kk: (round(vv, 5) if isinstance(vv, float) else vv) for kk, vv in v.items()}
-                                 for k, v in r["kernels"].items()}})
-        print(json.dumps(line), flush=True)
-
+        config.update({"ticks_per_step": cfg["ticks"], "grid": list(ADJ_GRID), "checkpoint_interval": ADJ_K,
+                       "hidden_factors": "U[0.7, 1.3] from the seed",
+                       "l2": "inputs larger than L2 (checkpoints and per-segment history)"})
+    return config
 
 if __name__ == "__main__":
     main()

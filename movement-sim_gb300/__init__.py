@@ -247,9 +247,20 @@ class Simulation:
                                    _ptr(out.get("speed"), ctypes.c_float)))
         return out
 
-    def get_neighbours(self, with_idx: bool = True):
-        count = np.empty(self.n, np.uint32)
-        idx = np.empty((self.n, self.cap), np.uint32) if (with_idx and self.cap) else None
+    def get_neighbours(self, with_idx: bool = True, out=None):
+        """(count (N,), idx (N, cap) or None) of the last neighbour tick; `out` = a
+        (count, idx) pair of arrays to fill instead of new ones."""
+        if out is not None:
+            count, idx = out
+            if count.dtype != np.uint32 or count.shape != (self.n,) or not count.flags.c_contiguous:
+                raise ValueError("out count must be a contiguous uint32 array of num_entities")
+            if not (with_idx and self.cap):
+                idx = None
+            elif idx.dtype != np.uint32 or idx.shape != (self.n, self.cap) or not idx.flags.c_contiguous:
+                raise ValueError("out idx must be a contiguous uint32 array of (num_entities, cap)")
+        else:
+            count = np.empty(self.n, np.uint32)
+            idx = np.empty((self.n, self.cap), np.uint32) if (with_idx and self.cap) else None
         check(lib().msim_get_neighbours(self._ctx, _ptr(count, ctypes.c_uint32), _ptr(idx, ctypes.c_uint32)))
         return count, idx
 

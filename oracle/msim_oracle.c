@@ -144,6 +144,180 @@ void oracle_init_entities(uint32_t num_roads, const float* road_pos, uint32_t n,
     }
 }
 
+/* ---- synthetic lattice road map ------------------------------------------------ */
+
+/* The synthetic L x L intersection lattice of the workloads, restated here so that
+ * the CPU legs need nothing of the product: node (a, b) at spacing*(a, b) plus a
+ * uniform offset in [0, 2*jitter) per axis (draw streams 10 and 11), the edge to
+ * (a+1, b) kept when draw stream 12 < keep_prob and the edge to (a, b+1) when
+ * stream 13 < keep_prob, the largest connected component kept (ties: the one
+ * holding the smallest node id).  Roads are numbered in node order, the edge to
+ * (a+1, b) before the edge to (a, b+1), and start at their lower node.  The
+ * connection lists follow map/generate_map.py:234-258: one list per node, every
+ * incident road once in ascending road id, a road that ENDS at the node appended a
+ * second time, and count = the number of distinct incident roads.  World size =
+ * largest endpoint coordinate + jitter (Map.cpp:42-52 maxDistLat/maxDistLong). */
+struct oracle_lattice {
+    uint32_t num_roads, num_conn;
+    float width, height;
+    float* road_pos;     /* 4 per road */
+    uint32_t* road_conn; /* 4 per road */
+    uint32_t* conn;
+};
+
+static int lattice_kept(uint64_t seed, uint64_t stream, uint64_t id, float keep_prob) {
+    return (double)(oracle_draw(seed, stream, id) >> 11) * 0x1p-53 < (double)keep_prob;
+}
+
+void oracle_lattice_free(oracle_lattice* m) {
+    if (!m) return;
+    free(m->road_pos);
+    free(m->road_conn);
+    free(m->conn);
+    free(m);
+}
+
+oracle_lattice* oracle_lattice_new(uint32_t side, uint64_t seed, float spacing, float jitter, float keep_prob) {
+    if (side < 2 || side > 8192 || !(spacing > 0.f) || !(jitter >= 0.f) || !(2.f * jitter < spacing) ||
+        !(keep_prob > 0.f) || keep_prob > 1.f)
+        return NULL;
+    const uint64_t L = side, nn = L * L;
+    float* nx = (float*)malloc(sizeof(float) * nn);
+    float* ny = (float*)malloc(sizeof(float) * nn);
+    uint8_t* edge = (uint8_t*)calloc(nn, 1); /* bit 0: to (a+1, b), bit 1: to (a, b+1) */
+    int32_t* label = (int32_t*)malloc(sizeof(int32_t) * nn);
+    uint32_t* queue = (uint32_t*)malloc(sizeof(uint32_t) * nn);
+    int64_t* road_h = (int64_t*)malloc(sizeof(int64_t) * nn);
+    int64_t* road_v = (int64_t*)malloc(sizeof(int64_t) * nn);
+    oracle_lattice* m = (oracle_lattice*)calloc(1, sizeof(oracle_lattice));
+    if (!nx || !ny || !edge || !label || !queue || !road_h || !road_v || !m) goto fail;
+    for (uint64_t id = 0; id < nn; id++) {
+        uint64_t a = id % L, b = id / L;
+        double ux = (double)(uint32_t)(oracle_draw(seed, 10, id) >> 40) * 0x1p-24;
+        double uy = (double)(uint32_t)(oracle_draw(seed, 11, id) >> 40) * 0x1p-24;
+        nx[id] = (float)((double)spacing * (double)a + 2.0 * (double)jitter * ux);
+        ny[id] = (float)((double)spacing * (double)b + 2.0 * (double)jitter * uy);
+        if (a + 1 < L && lattice_kept(seed, 12, id, keep_prob)) edge[id] |= 1;
+        if (b + 1 < L && lattice_kept(seed, 13, id, keep_prob)) edge[id] |= 2;
+    }
+    /* components by breadth-first search from the smallest unlabelled node: each
+     * component's first node is its smallest id, so the first largest one wins ties */
+    for (uint64_t id = 0; id < nn; id++) label[id] = -1;
+    int32_t best = -1, labels = 0;
+    uint64_t best_size = 0;
+    for (uint64_t s0 = 0; s0 < nn; s0++) {
+        if (label[s0] >= 0) continue;
+        uint64_t head = 0, tail = 0;
+        label[s0] = labels;
+        queue[tail++] = (uint32_t)s0;
+        while (head < tail) {
+            uint64_t v = queue[head++];
+            uint64_t a = v % L, b = v / L;
+            uint64_t nb[4];
+            int k = 0;
+            if (edge[v] & 1) nb[k++] = v + 1;
+            if (edge[v] & 2) nb[k++] = v + L;
+            if (a > 0 && (edge[v - 1] & 1)) nb[k++] = v - 1;
+            if (b > 0 && (edge[v - L] & 2)) nb[k++] = v - L;
+            for (int q = 0; q < k; q++)
+                if (label[nb[q]] < 0) {
+                    label[nb[q]] = labels;
+                    queue[tail++] = (uint32_t)nb[q];
+                }
+        }
+        if (tail > best_size) {
+            best_size = tail;
+            best = labels;
+        }
+        labels++;
+    }
+    if (best_size < 2) goto fail;
+    /* roads in node order */
+    uint64_t R = 0;
+    for (uint64_t id = 0; id < nn; id++) {
+        road_h[id] = road_v[id] = -1;
+        if (label[id] != best) continue;
+        if (edge[id] & 1) road_h[id] = (int64_t)R++;
+        if (edge[id] & 2) road_v[id] = (int64_t)R++;
+    }
+    m->num_roads = (uint32_t)R;
+    m->road_pos = (float*)malloc(sizeof(float) * 4 * R);
+    m->road_conn = (uint32_t*)calloc(4 * R, sizeof(uint32_t));
+    m->conn = (uint32_t*)malloc(sizeof(uint32_t) * 6 * R); /* <= 2 entries per road end */
+    if (!m->road_pos || !m->road_conn || !m->conn) goto fail;
+    float maxx = 0.f, maxy = 0.f;
+    for (uint64_t id = 0; id < nn; id++) {
+        for (int dir = 0; dir < 2; dir++) {
+            int64_t r = dir ? road_v[id] : road_h[id];
+            if (r < 0) continue;
+            uint64_t e = dir ? id + L : id + 1;
+            float* p = m->road_pos + 4 * r;
+            p[0] = nx[id];
+            p[1] = ny[id];
+            p[2] = nx[e];
+            p[3] = ny[e];
+            if (p[0] > maxx) maxx = p[0];
+            if (p[2] > maxx) maxx = p[2];
+            if (p[1] > maxy) maxy = p[1];
+            if (p[3] > maxy) maxy = p[3];
+        }
+    }
+    /* one connection list per node; incident roads ascending */
+    uint64_t C = 0;
+    for (uint64_t v = 0; v < nn; v++) {
+        uint64_t a = v % L, b = v / L;
+        int64_t inc[4];
+        int ends[4];
+        int d = 0;
+        if (b > 0 && road_v[v - L] >= 0) { inc[d] = road_v[v - L]; ends[d++] = 1; }
+        if (a > 0 && road_h[v - 1] >= 0) { inc[d] = road_h[v - 1]; ends[d++] = 1; }
+        if (road_h[v] >= 0) { inc[d] = road_h[v]; ends[d++] = 0; }
+        if (road_v[v] >= 0) { inc[d] = road_v[v]; ends[d++] = 0; }
+        if (d == 0) continue;
+        for (int i = 1; i < d; i++) /* insertion sort by road id */
+            for (int j = i; j > 0 && inc[j - 1] > inc[j]; j--) {
+                int64_t t = inc[j]; inc[j] = inc[j - 1]; inc[j - 1] = t;
+                int te = ends[j]; ends[j] = ends[j - 1]; ends[j - 1] = te;
+            }
+        uint32_t first = (uint32_t)C;
+        for (int q = 0; q < d; q++) {
+            uint32_t r = (uint32_t)inc[q];
+            m->conn[C++] = r;
+            if (ends[q]) {
+                m->conn[C++] = r;
+                m->road_conn[4ull * r + 2] = first;
+                m->road_conn[4ull * r + 3] = (uint32_t)d;
+            } else {
+                m->road_conn[4ull * r + 0] = first;
+                m->road_conn[4ull * r + 1] = (uint32_t)d;
+            }
+        }
+    }
+    m->num_conn = (uint32_t)C;
+    m->width = maxx + jitter;
+    m->height = maxy + jitter;
+    free(nx); free(ny); free(edge); free(label); free(queue); free(road_h); free(road_v);
+    return m;
+fail:
+    free(nx); free(ny); free(edge); free(label); free(queue); free(road_h); free(road_v);
+    oracle_lattice_free(m);
+    return NULL;
+}
+
+void oracle_lattice_info(const oracle_lattice* m, uint32_t* num_roads, uint32_t* num_conn, float* width,
+                         float* height) {
+    *num_roads = m->num_roads;
+    *num_conn = m->num_conn;
+    *width = m->width;
+    *height = m->height;
+}
+
+void oracle_lattice_copy(const oracle_lattice* m, float* road_pos, uint32_t* road_conn, uint32_t* conn) {
+    memcpy(road_pos, m->road_pos, sizeof(float) * 4ull * m->num_roads);
+    memcpy(road_conn, m->road_conn, sizeof(uint32_t) * 4ull * m->num_roads);
+    memcpy(conn, m->conn, sizeof(uint32_t) * m->num_conn);
+}
+
 /* ---- move step -------------------------------------------------------------- */
 
 typedef struct {

@@ -50,6 +50,15 @@ void oracle_init_entities(uint32_t num_roads, const float* road_pos, uint32_t n,
                           uint64_t seed, uint32_t placement, float speed_min, float speed_max,
                           float* pos, uint32_t* heading, uint32_t* rng, float* speed);
 
+/* Synthetic L x L lattice road map of the workloads (see msim_oracle.c for the
+ * rules); NULL on bad arguments or a lattice without edges. */
+typedef struct oracle_lattice oracle_lattice;
+oracle_lattice* oracle_lattice_new(uint32_t side, uint64_t seed, float spacing, float jitter, float keep_prob);
+void oracle_lattice_info(const oracle_lattice* m, uint32_t* num_roads, uint32_t* num_conn, float* width,
+                         float* height);
+void oracle_lattice_copy(const oracle_lattice* m, float* road_pos, uint32_t* road_conn, uint32_t* conn);
+void oracle_lattice_free(oracle_lattice* m);
+
 /* `ticks` move ticks of random_move.comp:830-852 (+ new_target 778-828) over all
  * n entities.  factor may be NULL (1.0).  threads <= 0 -> 1. */
 void oracle_step(uint32_t num_roads, const float* road_pos, const uint32_t* road_conn,

@@ -60,6 +60,12 @@ def lib():
         L.oracle_neighbours.restype = ctypes.c_uint64
         L.oracle_in_range.argtypes = [ctypes.c_float] * 5
         L.oracle_in_range.restype = ctypes.c_int
+        L.oracle_lattice_new.argtypes = [ctypes.c_uint32, ctypes.c_uint64, ctypes.c_float, ctypes.c_float,
+                                         ctypes.c_float]
+        L.oracle_lattice_new.restype = ctypes.c_void_p
+        L.oracle_lattice_info.argtypes = [ctypes.c_void_p, u32p, u32p, f32p, f32p]
+        L.oracle_lattice_copy.argtypes = [ctypes.c_void_p, f32p, u32p, u32p]
+        L.oracle_lattice_free.argtypes = [ctypes.c_void_p]
         _LIB = L
     return _LIB
 
@@ -87,6 +93,41 @@ def ref_lib():
 
 
 # ---- numpy conveniences -------------------------------------------------------
+
+class OracleMap:
+    """A road map as plain arrays: road_pos (R,4) f32, road_conn (R,4) u32,
+    connections (C,) u32, width, height (the fields the oracle's functions read)."""
+
+    def __init__(self, road_pos, road_conn, connections, width, height):
+        self.road_pos = road_pos
+        self.road_conn = road_conn
+        self.connections = connections
+        self.width = float(width)
+        self.height = float(height)
+
+    @property
+    def num_roads(self) -> int:
+        return int(self.road_pos.shape[0])
+
+
+def lattice(side: int, seed: int, spacing: float = 50.0, jitter: float = 10.0, keep_prob: float = 0.9) -> OracleMap:
+    """The synthetic side x side lattice road map of the workloads (msim_oracle.c)."""
+    L = lib()
+    h = L.oracle_lattice_new(side, seed, spacing, jitter, keep_prob)
+    if not h:
+        raise ValueError("lattice arguments rejected (side 2..8192, 0 <= 2 jitter < spacing, keep_prob in (0, 1])")
+    try:
+        R, C = ctypes.c_uint32(), ctypes.c_uint32()
+        w, hh = ctypes.c_float(), ctypes.c_float()
+        L.oracle_lattice_info(h, ctypes.byref(R), ctypes.byref(C), ctypes.byref(w), ctypes.byref(hh))
+        pos = np.empty((R.value, 4), np.float32)
+        conn = np.empty((R.value, 4), np.uint32)
+        cl = np.empty(C.value, np.uint32)
+        L.oracle_lattice_copy(h, _p(pos, ctypes.c_float), _p(conn, ctypes.c_uint32), _p(cl, ctypes.c_uint32))
+    finally:
+        L.oracle_lattice_free(h)
+    return OracleMap(pos, conn, cl, w.value, hh.value)
+
 
 def rng_seq(kind: int, state, n: int):
     s = np.array(state, dtype=np.uint32).copy()
@@ -137,11 +178,20 @@ def step(road_pos, road_conn, connections, pos, head, rng, speed, rng_kind, dt, 
                       _p(rng, ctypes.c_uint32), _p(speed, ctypes.c_float), threads or 1)
 
 
-def neighbours(pos, radius, cap, threads=None, with_idx=True):
+def neighbours(pos, radius, cap, threads=None, with_idx=True, out=None):
+    """(count, idx, pairs) of the CPU-grid query; `out` = (count, idx) arrays to reuse."""
     pos = np.ascontiguousarray(pos, dtype=np.float32)
     n = pos.shape[0]
-    count = np.zeros(n, np.uint32)
-    idx = np.zeros((n, cap), np.uint32) if (with_idx and cap) else None
+    if out is not None:
+        count, idx = out
+        assert count.dtype == np.uint32 and count.shape == (n,) and count.flags.c_contiguous
+        if not (with_idx and cap):
+            idx = None
+        else:
+            assert idx.dtype == np.uint32 and idx.shape == (n, cap) and idx.flags.c_contiguous
+    else:
+        count = np.zeros(n, np.uint32)
+        idx = np.zeros((n, cap), np.uint32) if (with_idx and cap) else None
     pairs = lib().oracle_neighbours(n, _p(pos, ctypes.c_float), radius, cap, _p(count, ctypes.c_uint32),
                                     _p(idx, ctypes.c_uint32), threads or 1)
     return count, idx, int(pairs)

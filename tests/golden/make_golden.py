@@ -1,7 +1,7 @@
 """Generates the committed golden fixtures from the reference (run where the
 reference tree is present; the fixtures travel with the repository).
 
-* test_map.npz     - /root/reference/test_map.json read with Python's json module
+* test_map.npz     - the reference's test_map.json read with Python's json module
                      and the loader rules of src/sim/Map.cpp:28-150 (numbers to
                      float32, zero-length roads skipped).
 * ref_quadtree.npz - entity sets and, per entity, the collision pairs (j < i)
@@ -13,11 +13,13 @@ reference tree is present; the fixtures travel with the repository).
                      the raw counter increments (which count repeated visits)
                      are stored.
 
-Usage: python tests/golden/make_golden.py
+Usage: python tests/golden/make_golden.py   (reference tree at $MSIM_REFERENCE_ROOT,
+default /root/reference, as oracle/build_oracle.py reads it)
 """
 from __future__ import annotations
 
 import json
+import os
 import sys
 from pathlib import Path
 
@@ -25,7 +27,7 @@ import numpy as np
 
 HERE = Path(__file__).resolve().parent
 ROOT = HERE.parent.parent
-REFERENCE = Path("/root/reference")
+REFERENCE = Path(os.environ.get("MSIM_REFERENCE_ROOT", "/root/reference"))
 sys.path.insert(0, str(ROOT))
 
 

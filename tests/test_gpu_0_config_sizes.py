@@ -1,0 +1,150 @@
+"""Parity of the timed path at the workload sizes, against the CPU oracle.
+
+The path under test is the one the benchmark times: the incremental index update,
+the query of tick t running on a second stream beside tick t+1's move and index
+update (double-buffered index), and the re-ordering of the state every 64 ticks.
+
+* 1,000,000 entities on the 256 x 256 lattice, radius 2 m, cap 64, all 500 ticks:
+  positions, headings, RNG states, neighbour counts and id lists compared after
+  every tick (the reference runs its collision dispatch after every move dispatch,
+  Simulator.cpp:227-235, random_move.comp:875-878).
+* The same workload advanced in multi-tick calls (the query overlaps the next
+  tick inside a call), compared at every call boundary, with the default
+  re-ordering interval and with a re-ordering every 5 ticks.
+* 16,000,000 entities on the 1024 x 1024 lattice for 135 ticks in multi-tick
+  calls: two re-orderings (before ticks 65 and 129) run under the overlap; full
+  state, counts and id lists compared just after each and at the end.
+
+Integer state and id lists must be equal; positions bit for bit (tolerance 0 m).
+This file sorts first among the GPU tests so that these runs happen even when a
+later test stops the run.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+SEED = 20261203
+DT = 0.1
+SPEED = (1.0, 1.6)
+RADIUS, CAP = 2.0, 64
+THREADS = 16
+
+
+def _compare(sim, orc, road_map, ost, buf, what):
+    pos, head, rng, _ = ost
+    st = sim.get_state(out=buf["state"])
+    assert np.array_equal(st["heading"], head), f"headings differ {what}"
+    assert np.array_equal(st["rng"], rng), f"RNG states differ {what}"
+    bad = np.nonzero(np.any(st["pos"].view(np.uint32) != pos.view(np.uint32), axis=1))[0]
+    assert bad.size == 0, f"positions differ {what}: {bad.size} entities, first {bad[:5]}"
+    cnt, idx = sim.get_neighbours(out=(buf["cnt"], buf["idx"]))
+    ocnt, oidx, opairs = orc.neighbours(pos, RADIUS, CAP, threads=THREADS, out=(buf["ocnt"], buf["oidx"]))
+    if not np.array_equal(cnt, ocnt):
+        bad = np.nonzero(cnt != ocnt)[0]
+        raise AssertionError(f"neighbour counts differ {what}: {bad.size} entities, first {bad[:5]} "
+                             f"{cnt[bad[:5]]} vs {ocnt[bad[:5]]}")
+    n = idx.shape[0]
+    step = 1 << 20  # row blocks: no full-size temporaries
+    for a in range(0, n, step):
+        if not np.array_equal(idx[a:a + step], oidx[a:a + step]):
+            rows = a + np.nonzero(np.any(idx[a:a + step] != oidx[a:a + step], axis=1))[0]
+            raise AssertionError(f"neighbour lists differ {what}: first rows {rows[:5]}")
+    assert sim.collision_pairs() == opairs, f"pair counter differs {what}"
+    return int(cnt.sum())
+
+
+def _host_available_bytes():
+    try:
+        with open("/proc/meminfo") as f:
+            for line in f:
+                if line.startswith("MemAvailable:"):
+                    return int(line.split()[1]) * 1024
+    except OSError:
+        pass
+    return None
+
+
+def _buffers(n):
+    return {"state": {"pos": np.empty((n, 2), np.float32), "heading": np.empty(n, np.uint32),
+                      "rng": np.empty((n, 4), np.uint32)},
+            "cnt": np.empty(n, np.uint32), "idx": np.empty((n, CAP), np.uint32),
+            "ocnt": np.empty(n, np.uint32), "oidx": np.empty((n, CAP), np.uint32)}
+
+
+def _setup(msim, orc, side, n, **kw):
+    road_map = msim.RoadMap.lattice(side, SEED)
+    sim = msim.Simulation(road_map, n, rng="pcg32", dt=DT, radius=RADIUS, cap=CAP, **kw)
+    sim.init_entities(SEED, placement="fraction", speed=SPEED)
+    ost = orc.init_entities(road_map.road_pos, n, 1, SEED, 1, SPEED[0], SPEED[1])
+    return road_map, sim, ost
+
+
+def _oracle_ticks(orc, road_map, ost, ticks):
+    pos, head, rng, speed = ost
+    orc.step(road_map.road_pos, road_map.road_conn, road_map.connections, pos, head, rng, speed, 1, DT, ticks,
+             threads=THREADS)
+
+
+def test_neighbours_config_every_tick_500(msim, orc):
+    """1 M entities, 256 x 256 lattice: every one of the 500 ticks compared in full."""
+    n, ticks = 1_000_000, 500
+    road_map, sim, ost = _setup(msim, orc, 256, n)
+    buf = _buffers(n)
+    links = 0
+    with sim:
+        assert sim.info()["resort_interval"] == 64
+        for t in range(ticks):
+            sim.step(1, neighbours=True)
+            _oracle_ticks(orc, road_map, ost, 1)
+            links += _compare(sim, orc, road_map, ost, buf, f"at tick {t + 1}")
+        assert sim.tick == ticks
+    assert links > 0
+    # road-end events with random choices happened
+    assert np.any(ost[2] != orc.init_entities(road_map.road_pos, n, 1, SEED, 1, SPEED[0], SPEED[1])[2])
+
+
+@pytest.mark.parametrize("resort", [0, 5])
+def test_neighbours_config_multi_tick_calls(msim, orc, resort):
+    """1 M entities for 500 ticks in calls of 2-12 ticks (query overlapping the next
+    tick inside each call); compared at every call boundary.  resort 0 = the
+    default interval (64), 5 = many re-orderings under the overlap."""
+    n, ticks = 1_000_000, 500
+    road_map, sim, ost = _setup(msim, orc, 256, n, resort_interval=resort)
+    buf = _buffers(n)
+    lengths = np.random.default_rng(resort + 1).integers(2, 13, ticks)
+    done = 0
+    with sim:
+        for k in lengths:
+            k = int(min(k, ticks - done))
+            if k == 0:
+                break
+            sim.step(k, neighbours=True)
+            _oracle_ticks(orc, road_map, ost, k)
+            done += k
+            _compare(sim, orc, road_map, ost, buf, f"at tick {done} (call of {k} ticks)")
+        assert done == ticks and sim.tick == ticks
+
+
+def test_scale_config_reorders_under_overlap(msim, orc):
+    """16 M entities, 1024 x 1024 lattice: 135 ticks in three multi-tick calls;
+    the re-orderings before ticks 65 and 129 run inside the calls.  Full state,
+    counts and id lists compared after ticks 65, 129 and 135."""
+    n = 16_000_000
+    avail = _host_available_bytes()
+    need = n * (2 * 4 * CAP + 64)  # two id-list arrays, states and counts
+    if avail is not None and avail < 2 * need:
+        pytest.skip(f"host memory: {avail >> 30} GiB available, the comparison needs about {need >> 30} GiB")
+    road_map, sim, ost = _setup(msim, orc, 1024, n)
+    buf = _buffers(n)
+    with sim:
+        info = sim.info()
+        assert info["resort_interval"] == 64 and info["sort_passes"] == 3
+        done = 0
+        for k in (65, 64, 6):
+            sim.step(k, neighbours=True)
+            _oracle_ticks(orc, road_map, ost, k)
+            done += k
+            links = _compare(sim, orc, road_map, ost, buf, f"at tick {done}")
+            assert links > 0
+        assert sim.tick == 135

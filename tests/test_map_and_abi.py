@@ -11,7 +11,16 @@ import numpy as np
 import pytest
 
 ROOT = Path(__file__).resolve().parent.parent
-REFERENCE_MAP = Path("/root/reference/test_map.json")
+
+
+def _reference_root() -> Path:
+    """Where the reference tree lies (the oracle's build recipe reads the same setting)."""
+    from oracle import build_oracle
+
+    return build_oracle.REFERENCE_ROOT
+
+
+REFERENCE_MAP = _reference_root() / "test_map.json"
 
 
 def test_header_symbols_exported(msim):
@@ -201,3 +210,19 @@ def test_quad_tree_export_matches_reference(msim, orc, golden_dir):
             assert np.array_equal(mn.view(np.uint32).reshape(-1, 16), rn)
             assert np.array_equal(ml.view(np.uint32).reshape(-1, 5), rl)
     assert msim.node_count(8) == 21845 and msim.node_count(1) == 1 and msim.node_count(4) == 85
+
+
+@pytest.mark.parametrize("side,seed,keep", [(2, 1, 0.9), (3, 5, 0.9), (16, 7, 0.9), (32, 20261203, 0.9),
+                                            (40, 9, 0.3), (40, 9, 1.0), (256, 20261203, 0.9),
+                                            (1024, 20261203, 0.9)])
+def test_oracle_lattice_equals_product_lattice(msim, orc, side, seed, keep):
+    """The oracle's own lattice generator (used by the CPU baseline and the reference
+    arm, which load nothing of the product) gives the product's map bit for bit."""
+    a = orc.lattice(side, seed, keep_prob=keep)
+    b = msim.RoadMap.lattice(side, seed, keep_prob=keep)
+    assert np.array_equal(a.road_pos.view(np.uint32), b.road_pos.view(np.uint32))
+    assert np.array_equal(a.road_conn, b.road_conn)
+    assert np.array_equal(a.connections, b.connections)
+    assert (a.width, a.height) == (b.width, b.height)
+    with pytest.raises(ValueError):
+        orc.lattice(1, seed)

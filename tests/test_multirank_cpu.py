@@ -70,3 +70,39 @@ def test_reference_arm_under_torchrun_two_ranks():
     line = json.loads(lines[0])
     assert line["impl"] == "reference" and line["metric"] == "entity-steps/s" and line["value"] > 0
     assert line["cpu_baseline"]["kind"] == "port" and line["e2e"]["h2d_bytes_per_step"] == 0
+
+
+def test_reference_arm_loads_only_the_oracle_and_prints_the_same_config():
+    """The reference arm runs the oracle on the GPU arm's own workload and loads no
+    library of the product; its config dict is the GPU arm's (nothing measured in it)."""
+    code = ("import sys, json, io, contextlib; sys.path.insert(0, '.'); import bench;"
+            "sys.argv = ['bench.py', '--impl', 'reference', '--config', 'neighbours', '--entities', '50000',"
+            " '--lattice', '64', '--steps', '2', '--warmup', '3'];"
+            "buf = io.StringIO();"
+            "ctx = contextlib.redirect_stdout(buf); ctx.__enter__(); bench.main(); ctx.__exit__(None, None, None);"
+            "maps = open('/proc/self/maps').read();"
+            "print(json.dumps({'line': json.loads(buf.getvalue().strip().splitlines()[-1]),"
+            " 'libmsim': 'libmsim' in maps, 'oracle': 'liboracle' in maps,"
+            " 'pkg': any(m.startswith('movement-sim_gb300') for m in sys.modules)}))")
+    res = subprocess.run([sys.executable, "-c", code], cwd=ROOT, capture_output=True, text=True, timeout=600,
+                         env=dict(os.environ, CUDA_VISIBLE_DEVICES=""))
+    assert res.returncode == 0, res.stderr[-2000:]
+    out = json.loads(res.stdout.strip().splitlines()[-1])
+    assert out["oracle"] and not out["libmsim"] and not out["pkg"]
+    line = out["line"]
+    assert line["impl"] == "reference" and line["value"] > 0
+    sys.path.insert(0, str(ROOT))
+    import argparse
+
+    import bench
+
+    args = argparse.Namespace(config="neighbours", entities=50000, lattice=64, cap=None, ticks=None, instances=512)
+    cfg = dict(bench.CONFIGS["neighbours"], entities=50000, lattice=64)
+    assert line["config"] == bench.workload_config(args, cfg, 1)
+
+
+def test_bench_ensemble_matches_package(msim):
+    sys.path.insert(0, str(ROOT))
+    import bench
+
+    assert bench.ensemble_config(512) == msim.ensemble_config(512)
