@@ -374,7 +374,8 @@ def run_batched(args, world, rank, local):
     batch = pkg.Batch(maps, ents, rng="pcg32", dt=DT)
     batch.init_entities(seeds, placement="fraction", speed=SPEED)
     t_tune = time.perf_counter()
-    batch.tune(min(args.steps, 100), args.tune_cache)
+    if not args.no_tune:
+        batch.tune(min(args.steps, 100), args.tune_cache)
     t_tune = time.perf_counter() - t_tune
     batch.init_entities(seeds, placement="fraction", speed=SPEED)
     batch.step(args.steps)  # warm-up: builds the graph for this tick count
@@ -441,16 +442,37 @@ def run_batched(args, world, rank, local):
                                  "per entity per launch); see issue"}}
 
 
+def run_facade(cfg, ticks=200, warmup=5):
+    """The drop-in C++ façade (sim::Simulator::tick_once, one synchronous tick per
+    call with its phase times, CSV log line and pair counter) on the workload, run by
+    the example program movement-sim_gb300/examples/simulator_ticks."""
+    exe = ROOT / "movement-sim_gb300" / "examples" / "simulator_ticks"
+    if not exe.exists():
+        return {"unavailable": f"{exe.name} not built"}
+    with tempfile.TemporaryDirectory() as td:
+        r = subprocess.run([str(exe), str(cfg["lattice"]), str(cfg["entities"]), str(ticks), str(warmup),
+                            str(Path(td) / "ticks.csv")], capture_output=True, text=True, timeout=600)
+    if r.returncode != 0:
+        return {"error": (r.stderr or r.stdout)[-400:]}
+    out = json.loads(r.stdout.strip().splitlines()[-1])
+    out["what"] = (f"sim::Simulator::tick_once x {ticks} after {warmup} warm-up ticks ({cfg['entities']} entities, "
+                   f"{cfg['lattice']}x{cfg['lattice']} lattice): msim_step(1) + msim_sync + phase times + CSV log "
+                   "line per tick")
+    return out
+
+
 def run_forms(args, world, rank, local):
     """Short runs of the two other forms, added to the default line: the batched
     ensemble (512 instances, 1,000 ticks in one launch, against one-at-a-time
     launches) and the calibration step (forward + adjoint, 2 steps after 1 warm-up)."""
     a = argparse.Namespace(**vars(args))
-    a.steps, a.warmup, a.no_e2e, a.no_cpu, a.ticks = CONFIGS["batched"]["ticks"], 3, True, True, None
+    a.steps, a.warmup, a.no_e2e, a.no_cpu, a.ticks, a.no_tune = CONFIGS["batched"]["ticks"], 3, True, True, None, False
     b = run_batched(a, world, rank, local)
     a.steps, a.warmup = 2, 1
     d = run_adjoint(a, world, rank, local)
-    return {"batched": {"workload": "512 instances, lattice side U{16..256}, entities log-U[1e3, 2e5], "
+    f = run_facade(CONFIGS["scale"])
+    return {"facade": f,
+            "batched": {"workload": "512 instances, lattice side U{16..256}, entities log-U[1e3, 2e5], "
                                     f"{b['total_entities']} entities, 1,000 ticks in one launch",
                         "value": b["value"], "unit": "entity-steps/s", "ms_per_tick": b["ms_per_step"],
                         "one_at_a_time": b["one_at_a_time"]["value"],
@@ -706,6 +728,7 @@ def main():
     ap.add_argument("--ticks", type=int, default=None, help="adjoint config: ticks per step (profiling runs)")
     ap.add_argument("--instances", type=int, default=512, help="batched config: number of instances")
     ap.add_argument("--tune-cache", default=None, help="batched config: tuner cache file to reuse/append")
+    ap.add_argument("--no-tune", action="store_true", help="batched config: the default schedule (profiling runs)")
     ap.add_argument("--cpu-entities", type=int, default=None,
                     help="adjoint config: entities of the CPU adjoint (default: the workload's)")
     args = ap.parse_args()

@@ -174,8 +174,17 @@ int msim_set_road_factors(msim_ctx* ctx, const float* factors);
 int msim_step(msim_ctx* ctx, uint32_t ticks, uint32_t flags);
 
 /* Waits for queued work (the fence wait inside kp::Sequence::eval) and reports
- * device-side errors recorded since the last call. */
+ * device-side errors recorded since the last call.  MSIM_ERR_TIMEOUT: a bounded
+ * device wait of the spatial index gave up (see msim_set_wait_limit); the kernels
+ * that read the index then skipped their work, so the entity state is intact but
+ * the neighbour results of the ticks since the last successful sync are not; the
+ * next neighbour tick rebuilds the index from scratch. */
 int msim_sync(msim_ctx* ctx);
+
+/* No counterpart in the reference (it has no failure detection).  Polls of a
+ * look-back word by the index kernels before a wait gives up and the tick reports
+ * MSIM_ERR_TIMEOUT (default 2^24, about a second; 0 restores the default). */
+int msim_set_wait_limit(msim_ctx* ctx, uint32_t polls);
 
 /* Replaces the device->host readback of the entity buffer (Simulator.cpp:248-263):
  * any pointer may be NULL.  Synchronous. */
@@ -261,7 +270,19 @@ int msim_get_tick(msim_ctx* ctx, uint64_t* tick);
 /* Kernels this context has launched since msim_create (all kinds). */
 int msim_get_launch_count(msim_ctx* ctx, uint64_t* launches);
 
-/* Device-side timing of the context's kernels (CUDA events on its stream). */
+/* Per-tick phase times, the counterpart of the per-dispatch timers of
+ * Simulator::sim_tick (Simulator.cpp:213-237: update = move dispatch, collision =
+ * collision dispatch).  With enable, every neighbour tick records three events on
+ * the streams that run its phases (before the move, after the move, after the
+ * query), which keeps the query on its own stream; msim_get_tick_times waits for
+ * the last neighbour tick and returns its update time (move, plus the occasional
+ * re-ordering of the state) and its collision time (index update and query). */
+int msim_set_tick_timing(msim_ctx* ctx, int enable);
+int msim_get_tick_times(msim_ctx* ctx, float* update_ms, float* collision_ms);
+
+/* Device-side timing of the context's kernels (CUDA events on its stream, one pair
+ * per launch; the query then runs on the context's main stream, serialised with the
+ * next tick, so kernel times do not overlap). */
 int msim_set_profiling(msim_ctx* ctx, int enable);
 int msim_reset_kernel_stats(msim_ctx* ctx);
 /* kernel: 0 .. msim_kernel_count()-1.  Synchronises the context's stream. */

@@ -156,6 +156,10 @@ struct SimulatorConfig {
     float collision_radius = COLLISION_RADIUS;
     uint32_t neighbour_cap = 64;
     std::filesystem::path log_csv_path;  // empty -> "<num_entities>.csv" (Simulator.cpp:337-340)
+    // Per-kernel device times (msim_get_kernel_stats) cost an event pair per launch and
+    // serialise the query with the next tick; the update / collision histories come
+    // from per-tick phase events (msim_set_tick_timing) either way.
+    bool kernel_stats = false;
 };
 
 class Simulator {
@@ -226,7 +230,6 @@ class Simulator {
     bool want_entities_{true};
     bool want_nodes_{true};
     uint64_t collision_pairs_{0};
-    double last_update_ms_{0}, last_collision_ms_{0};
 };
 
 }  // namespace sim

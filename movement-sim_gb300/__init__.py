@@ -294,6 +294,14 @@ class Simulation:
         check(lib().msim_get_launch_count(self._ctx, ctypes.byref(v)))
         return v.value
 
+    def set_wait_limit(self, polls: int) -> None:
+        """Polls before a bounded device wait of the index gives up (0: the default)."""
+        check(lib().msim_set_wait_limit(self._ctx, polls))
+
+    def inject_fault(self, fault: int, arg: int = 0) -> None:
+        """Arms one host-side fault (msim_debug.h: FAULT_SORT_TILE, FAULT_LAUNCH)."""
+        check(lib().msim_debug_inject(self._ctx, fault, arg))
+
     def set_profiling(self, on: bool) -> None:
         check(lib().msim_set_profiling(self._ctx, 1 if on else 0))
 

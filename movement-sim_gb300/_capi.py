@@ -29,6 +29,9 @@ STEP_NEIGHBOURS = 1
 PARAM_FULL_SORT = 1
 PARAM_INCREMENTAL = 2
 NO_NEIGHBOUR = 0xFFFFFFFF
+FAULT_NONE = 0
+FAULT_SORT_TILE = 1
+FAULT_LAUNCH = 2
 
 
 class MsimError(RuntimeError):
@@ -72,6 +75,11 @@ SIGNATURES = {
     "msim_map_write_json": (ctypes.c_int, [ctypes.POINTER(MsimMap), ctypes.c_char_p]),
     "msim_map_validate": (ctypes.c_int, [ctypes.POINTER(MsimMap)]),
     "msim_map_free": (None, [vp]),
+    "msim_set_wait_limit": (ctypes.c_int, [vp, c_u32]),
+    "msim_set_tick_timing": (ctypes.c_int, [vp, ctypes.c_int]),
+    "msim_get_tick_times": (ctypes.c_int, [vp, f32p, f32p]),
+    "msim_debug_inject": (ctypes.c_int, [vp, c_u32, c_u32]),
+    "msim_debug_fail_device_alloc": (ctypes.c_int, [ctypes.c_int64]),
     "msim_create": (ctypes.c_int, [ctypes.POINTER(MsimMap), ctypes.POINTER(MsimParams), ctypes.POINTER(vp)]),
     "msim_destroy": (ctypes.c_int, [vp]),
     "msim_init_entities": (ctypes.c_int, [vp, ctypes.POINTER(MsimInit)]),

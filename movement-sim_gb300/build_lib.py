@@ -84,7 +84,24 @@ def build(verbose: bool = False, extra_nvcc: list[str] | None = None) -> Path:
         if res.returncode != 0:
             raise RuntimeError("libmsim link failed:\n" + res.stdout)
         os.replace(tmp, LIB)
+    build_examples(verbose)
     return LIB
+
+
+def build_examples(verbose: bool = False) -> None:
+    """Host-only C++ programs over the façade (examples/*.cpp), linked to libmsim.so."""
+    for src in sorted((PKG / "examples").glob("*.cpp")):
+        exe = PKG / "examples" / src.stem
+        deps = [src, LIB, *(ROOT / "include").glob("*.hpp"), *(ROOT / "include").glob("*.h")]
+        if exe.exists() and all(exe.stat().st_mtime >= d.stat().st_mtime for d in deps):
+            continue
+        cmd = [os.environ.get("CXX", "g++"), "-std=c++17", "-O2", "-Wall", "-I", str(ROOT / "include"), str(src),
+               "-L", str(PKG), "-lmsim", f"-Wl,-rpath,{PKG}", "-pthread", "-o", str(exe)]
+        if verbose:
+            print(" ".join(cmd), flush=True)
+        res = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
+        if res.returncode != 0:
+            raise RuntimeError(f"example {src.name} failed to build:\n" + res.stdout)
 
 
 if __name__ == "__main__":

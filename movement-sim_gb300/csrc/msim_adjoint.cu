@@ -542,11 +542,8 @@ namespace {
 template <typename T>
 int aalloc(msim_adj* a, T** ptr, size_t count) {
     void* raw = nullptr;
-    cudaError_t e = cudaMalloc(&raw, std::max<size_t>(count, 1) * sizeof(T));
-    if (e != cudaSuccess) {
-        cudaGetLastError();
-        return fail(MSIM_ERR_NOMEM, "cudaMalloc failed in the adjoint context: " + std::string(cudaGetErrorString(e)));
-    }
+    if (!device_malloc(&raw, std::max<size_t>(count, 1) * sizeof(T)))
+        return fail(MSIM_ERR_NOMEM, "device allocation failed in the adjoint context");
     a->allocs.push_back(raw);
     *ptr = static_cast<T*>(raw);
     return MSIM_OK;

@@ -183,11 +183,8 @@ namespace {
 template <typename T>
 int balloc(msim_batch* b, T** p, size_t count) {
     void* raw = nullptr;
-    cudaError_t e = cudaMalloc(&raw, std::max<size_t>(count, 1) * sizeof(T));
-    if (e != cudaSuccess) {
-        cudaGetLastError();
-        return fail(MSIM_ERR_NOMEM, "cudaMalloc failed in the batch: " + std::string(cudaGetErrorString(e)));
-    }
+    if (!device_malloc(&raw, std::max<size_t>(count, 1) * sizeof(T)))
+        return fail(MSIM_ERR_NOMEM, "device allocation failed in the batch");
     b->allocs.push_back(raw);
     *p = static_cast<T*>(raw);
     return MSIM_OK;
@@ -565,8 +562,9 @@ int msim_batch_tune(msim_batch* b, uint32_t ticks, const char* cache_path) {
     float2* sp = nullptr;
     uint32_t* sh = nullptr;
     uint4* sr = nullptr;
-    if (cudaMalloc(&sp, sizeof(float2) * T) != cudaSuccess || cudaMalloc(&sh, sizeof(uint32_t) * T) != cudaSuccess ||
-        cudaMalloc(&sr, sizeof(uint4) * T) != cudaSuccess) {
+    if (!device_malloc(reinterpret_cast<void**>(&sp), sizeof(float2) * T) ||
+        !device_malloc(reinterpret_cast<void**>(&sh), sizeof(uint32_t) * T) ||
+        !device_malloc(reinterpret_cast<void**>(&sr), sizeof(uint4) * T)) {
         cudaFree(sp);
         cudaFree(sh);
         cudaFree(sr);

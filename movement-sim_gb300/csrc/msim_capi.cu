@@ -1,6 +1,7 @@
 // C ABI of the movement-sim per-tick path: context lifecycle, tick orchestration
 // on the context's CUDA stream, exports back to the reference's layouts.
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstring>
 #include <new>
@@ -9,6 +10,7 @@
 
 #include <cuda_runtime.h>
 
+#include "msim_debug.h"
 #include "msim_internal.h"
 #include "msim_kernels.cuh"
 
@@ -20,6 +22,25 @@ void set_error(const std::string& msg) { g_last_error = msg; }
 int fail(int code, const std::string& msg) {
     g_last_error = msg;
     return code;
+}
+
+// Device allocations left before an injected failure (msim_debug_fail_device_alloc);
+// negative: no failure injected.
+static std::atomic<long long> g_alloc_budget{-1};
+
+bool device_malloc(void** p, size_t bytes) {
+    *p = nullptr;
+    long long b = g_alloc_budget.load();
+    while (b >= 0) {
+        if (b == 0) return false;  // injected: every allocation fails until reset
+        if (g_alloc_budget.compare_exchange_weak(b, b - 1)) break;
+    }
+    if (cudaMalloc(p, bytes) != cudaSuccess) {
+        cudaGetLastError();
+        *p = nullptr;
+        return false;
+    }
+    return true;
 }
 
 enum KernelId : uint32_t {
@@ -49,6 +70,8 @@ using namespace msim;
 
 struct msim_ctx {
     int device = 0;
+    uint32_t spin_limit = kDefaultSpinLimit;  // polls before a bounded device wait gives up
+    uint32_t fault = 0, fault_arg = 0;        // injected fault (msim_debug_inject), one shot
     cudaStream_t stream = nullptr;
     msim_params params{};
     uint32_t n = 0, R = 0, C = 0;
@@ -136,6 +159,12 @@ struct msim_ctx {
     double ms[K_COUNT] = {};
     cudaEvent_t t0 = nullptr, t1 = nullptr;
     bool timer_open = false;
+    // per-tick phase events (msim_set_tick_timing): before the move, after it, after
+    // the query; recorded on the stream that runs each phase, so the query keeps its
+    // own stream
+    bool tick_timing = false;
+    bool tick_recorded = false;
+    cudaEvent_t ev_tick[3] = {nullptr, nullptr, nullptr};
     // the query of tick t runs on qstream while the main stream moves tick t + 1
     cudaStream_t qstream = nullptr;
     cudaEvent_t ev_index = nullptr;  // key-start table and sorted positions of tick t ready
@@ -170,18 +199,17 @@ int cuda_fail(cudaError_t e, const char* what) {
         cudaError_t e_ = (expr);                         \
         if (e_ != cudaSuccess) return cuda_fail(e_, what); \
     } while (0)
+// A launch of a tick's kernel under a Prof p: an injected fault (MSIM_FAULT_LAUNCH)
+// reports a launch failure instead of issuing it.
+#define CKL(p, expr, what) CK(inject_launch((p).c) ? cudaErrorLaunchFailure : (expr), what)
 
 template <typename T>
 int dalloc(msim_ctx* c, T** p, size_t count) {
     *p = nullptr;
     if (count == 0) count = 1;
     void* raw = nullptr;
-    cudaError_t e = cudaMalloc(&raw, count * sizeof(T));
-    if (e != cudaSuccess) {
-        cudaGetLastError();
-        return fail(MSIM_ERR_NOMEM, "cudaMalloc of " + std::to_string(count * sizeof(T)) + " bytes failed: " +
-                                        cudaGetErrorString(e));
-    }
+    if (!device_malloc(&raw, count * sizeof(T)))
+        return fail(MSIM_ERR_NOMEM, "device allocation of " + std::to_string(count * sizeof(T)) + " bytes failed");
     c->allocs.push_back(raw);
     c->device_bytes += count * sizeof(T);
     *p = static_cast<T*>(raw);
@@ -203,6 +231,8 @@ void free_all(msim_ctx* c) {
     if (c->t0) cudaEventDestroy(c->t0);
     if (c->t1) cudaEventDestroy(c->t1);
     if (c->ev_index) cudaEventDestroy(c->ev_index);
+    for (int k = 0; k < 3; k++)
+        if (c->ev_tick[k]) cudaEventDestroy(c->ev_tick[k]);
     for (int b = 0; b < 2; b++)
         if (c->ev_read[b]) cudaEventDestroy(c->ev_read[b]);
     if (c->qstream) cudaStreamDestroy(c->qstream);
@@ -225,6 +255,17 @@ cudaEvent_t pool_event(msim_ctx* c) {
     cudaEvent_t e = nullptr;
     cudaEventCreate(&e);
     return e;
+}
+
+// An injected launch failure (MSIM_FAULT_LAUNCH): true for the launch it names.
+bool inject_launch(msim_ctx* c) {
+    if (c->fault != MSIM_FAULT_LAUNCH) return false;
+    if (c->fault_arg > 0) {
+        c->fault_arg--;
+        return false;
+    }
+    c->fault = 0;
+    return true;
 }
 
 // Records an event pair around one launch when profiling is on.
@@ -268,12 +309,8 @@ int ensure_stage(msim_ctx* c, size_t bytes) {
     if (c->stage) cudaFree(c->stage);
     c->stage = nullptr;
     c->stage_bytes = 0;
-    cudaError_t e = cudaMalloc(&c->stage, bytes);
-    if (e != cudaSuccess) {
-        cudaGetLastError();
-        c->stage = nullptr;
-        return fail(MSIM_ERR_NOMEM, "cudaMalloc of export staging (" + std::to_string(bytes) + " bytes) failed");
-    }
+    if (!device_malloc(&c->stage, bytes))
+        return fail(MSIM_ERR_NOMEM, "device allocation of export staging (" + std::to_string(bytes) + " bytes) failed");
     c->stage_bytes = bytes;
     return MSIM_OK;
 }
@@ -358,13 +395,25 @@ int clear_unchained(msim_ctx* c) {
 
 int sort_keys(msim_ctx* c);
 
+// MSIM_FAULT_SORT_TILE: the look-back chain about to start (the ticket that hands out
+// its tiles) begins at tile 1, so tile 0 is never processed and tile 1's bounded
+// wait for it runs out.
+int inject_sort_tile(msim_ctx* c, uint32_t* ticket) {
+    if (c->fault != MSIM_FAULT_SORT_TILE) return MSIM_OK;
+    c->fault = 0;
+    static const uint32_t one = 1u;
+    CK(cudaMemcpyAsync(ticket, &one, sizeof(one), cudaMemcpyHostToDevice, c->stream), "inject sort fault");
+    return MSIM_OK;
+}
+
 // key + histogram (of the current positions, or after one move tick) + radix sort
 int sort_entities(msim_ctx* c, uint32_t move_ticks) {
     CK(cudaMemsetAsync(c->hist, 0, sizeof(uint32_t) * kMaxPasses * kRadix, c->stream), "memset hist");
     {
         Prof p(c, K_STEP);
-        CK(launch_step(c->stream, step_args(c, move_ticks, true)), "k_step");
+        CKL(p, launch_step(c->stream, step_args(c, move_ticks, true)), "k_step");
     }
+    if (c->tick_timing && move_ticks) CK(cudaEventRecord(c->ev_tick[1], c->stream), "cudaEventRecord");
     return sort_keys(c);
 }
 
@@ -374,15 +423,16 @@ int sort_keys(msim_ctx* c) {
     if (rc != MSIM_OK) return rc;
     rc = join_query(c);  // the passes rewrite the sorted slots the last query reads
     if (rc != MSIM_OK) return rc;
+    if ((rc = inject_sort_tile(c, c->tickets)) != MSIM_OK) return rc;
     c->chain_broken = true;  // until every pass has launched
     for (uint32_t ps = 0; ps < c->passes; ps++) {
         const uint32_t* kin = ps == 0 ? c->key : c->sk[(ps - 1) & 1];
         const uint32_t* vin = ps == 0 ? nullptr : c->sv[(ps - 1) & 1];
         const SweepChain ch = sweep_chain(c, ps);
         Prof p(c, K_SORT_PASS);
-        CK(launch_onesweep(c->stream, kin, vin, c->sk[ps & 1], c->sv[ps & 1], c->n, 8u * ps,
+        CKL(p, launch_onesweep(c->stream, kin, vin, c->sk[ps & 1], c->sv[ps & 1], c->n, 8u * ps,
                            c->hist + ps * kRadix, c->lookback + ps * c->sort_region, c->tickets + ps, c->err,
-                           nullptr, c->passes >= 2 ? &ch : nullptr),
+                           nullptr, c->passes >= 2 ? &ch : nullptr, c->spin_limit),
            "k_onesweep");
     }
     c->chain_broken = false;
@@ -399,7 +449,7 @@ int permute_state(msim_ctx* c) {
     int rc = join_query(c);
     if (rc != MSIM_OK) return rc;
     Prof p(c, K_PERMUTE);
-    CK(launch_permute(c->stream, c->sorted_slot, c->st[c->cur], c->st[1 - c->cur], c->n), "k_permute");
+    CKL(p, launch_permute(c->stream, c->sorted_slot, c->st[c->cur], c->st[1 - c->cur], c->n, c->err), "k_permute");
     c->cur = 1 - c->cur;
     c->have_sort = false;
     c->order_identity = true;  // slot q now holds the entity at sorted position q
@@ -448,31 +498,34 @@ int incremental_index(msim_ctx* c) {
         Prof p(c, K_STEP);
         StepLaunch a = step_args(c, 1, true);
         a.hist = nullptr;  // the changed keys' digits are counted by k_mark
-        CK(launch_step(c->stream, a), "k_step");
+        CKL(p, launch_step(c->stream, a), "k_step");
     }
+    if (c->tick_timing) CK(cudaEventRecord(c->ev_tick[1], c->stream), "cudaEventRecord");
     return incremental_update(c);
 }
 
 // The update itself, for new keys (by slot) already in c->key.
 int incremental_update(msim_ctx* c) {
+    int rc = inject_sort_tile(c, c->mark_ticket);
+    if (rc != MSIM_OK) return rc;
     {
         Prof p(c, K_MARK);
-        CK(launch_mark(c->stream, c->sorted_slot, c->order_identity, c->sorted_key, c->key, c->n, c->passes,
+        CKL(p, launch_mark(c->stream, c->sorted_slot, c->order_identity, c->sorted_key, c->key, c->n, c->passes,
                        c->a_key, c->a_val, c->b_key[0], c->b_val[0], c->hist, c->mark_lookback, c->mark_ticket,
-                       c->ab_counts, c->err, c->sorted_dev),
+                       c->ab_counts, c->err, c->sorted_dev, c->spin_limit),
            "k_mark");
         c->index_updates++;
     }
-    int rc = clear_unchained(c);
+    rc = clear_unchained(c);
     if (rc != MSIM_OK) return rc;
     c->chain_broken = true;  // until every pass has launched
     for (uint32_t ps = 0; ps < c->passes; ps++) {  // stable radix sort of the changed entries
         const SweepChain ch = sweep_chain(c, ps);
         Prof p(c, K_SORT_PASS);
-        CK(launch_onesweep(c->stream, c->b_key[ps & 1], c->b_val[ps & 1], c->b_key[(ps + 1) & 1],
+        CKL(p, launch_onesweep(c->stream, c->b_key[ps & 1], c->b_val[ps & 1], c->b_key[(ps + 1) & 1],
                            c->b_val[(ps + 1) & 1], c->n, 8u * ps, c->hist + ps * kRadix,
                            c->lookback + ps * c->sort_region, c->tickets + ps, c->err, c->ab_counts + 1,
-                           c->passes >= 2 ? &ch : nullptr),
+                           c->passes >= 2 ? &ch : nullptr, c->spin_limit),
            "k_onesweep");
     }
     c->chain_broken = false;
@@ -485,7 +538,7 @@ int incremental_update(msim_ctx* c) {
     {
         Prof p(c, K_MERGE);
         uint32_t launched = 0;
-        CK(launch_merge(c->stream, c->a_key, c->a_val, c->b_key[c->passes & 1], c->b_val[c->passes & 1],
+        CKL(p, launch_merge(c->stream, c->a_key, c->a_val, c->b_key[c->passes & 1], c->b_val[c->passes & 1],
                         c->ab_counts, c->merge_split, c->n, c->sk[out], c->sv[out], cur_state(c).pos, c->sorted_pos,
                         c->kstart, (uint32_t)c->num_keys, c->kstart_chunks, c->kstart_chunk_count, c->err,
                         &launched),
@@ -504,6 +557,7 @@ int run_query(msim_ctx* c, bool overlap);
 
 int neighbour_tick(msim_ctx* c) {
     int rc;
+    if (c->tick_timing) CK(cudaEventRecord(c->ev_tick[0], c->stream), "cudaEventRecord");
     if (c->have_sort && c->since_permute >= c->resort) {
         rc = permute_state(c);
         if (rc != MSIM_OK) return rc;
@@ -527,8 +581,8 @@ int key_start_table(msim_ctx* c) {
     use_index_buffers(c, c->sorted_slot == c->sv[0] ? 0 : 1);
     Prof p(c, K_KSTART);
     uint32_t launched = 0;
-    CK(launch_kstart(c->stream, c->sorted_key, c->n, c->kstart, (uint32_t)c->num_keys, c->kstart_chunks,
-                     c->kstart_chunk_count, &launched, c->sorted_slot, cur_state(c).pos, c->sorted_pos),
+    CKL(p, launch_kstart(c->stream, c->sorted_key, c->n, c->kstart, (uint32_t)c->num_keys, c->kstart_chunks,
+                     c->kstart_chunk_count, &launched, c->sorted_slot, cur_state(c).pos, c->sorted_pos, c->err),
        "k_kstart");
     if (launched > 1) c->launch_count += launched - 1;
     return MSIM_OK;
@@ -549,14 +603,18 @@ int run_query(msim_ctx* c, bool overlap) {
     {
         Prof p(c, K_QUERY);
         // slots that hold their own entity need no id lookup
-        CK(launch_query(qs, c->params.cap, c->kstart, c->sorted_slot, c->sorted_pos,
+        CKL(p, launch_query(qs, c->params.cap, c->kstart, c->sorted_slot, c->sorted_pos,
                         c->slots_identity ? nullptr : cur_state(c).slot_id, c->grid,
-                        c->n, c->nbr_count, c->nbr_list, c->pairs),
+                        c->n, c->nbr_count, c->nbr_list, c->pairs, c->err),
            "k_query");
     }
     if (qs != c->stream) {
         CK(cudaEventRecord(c->ev_read[c->ib], qs), "cudaEventRecord");
         c->read_pending[c->ib] = true;
+    }
+    if (c->tick_timing) {
+        CK(cudaEventRecord(c->ev_tick[2], qs), "cudaEventRecord");
+        c->tick_recorded = true;
     }
     c->have_nbr = true;
     c->since_permute++;
@@ -576,8 +634,15 @@ int sync_and_check(msim_ctx* c) {
     CK(cudaMemcpy(&h, c->err, sizeof(h), cudaMemcpyDeviceToHost), "read device status");
     if (h) {
         CK(cudaMemsetAsync(c->err, 0, sizeof(uint32_t), c->stream), "clear device status");
-        if (h & kErrTimeout)
-            return fail(MSIM_ERR_TIMEOUT, "a bounded device wait (radix sort look-back) gave up; results of the tick are invalid");
+        if (h & kErrTimeout) {
+            // The kernels that read the index skipped their work after the wait gave
+            // up, so the entity state is intact; the index is rebuilt from scratch (full
+            // sort, every look-back region zeroed again) by the next neighbour tick.
+            c->chain_broken = true;
+            reset_index(c);
+            return fail(MSIM_ERR_TIMEOUT, "a bounded device wait (index look-back) gave up; the neighbour results "
+                                          "since the last successful sync are invalid, the entity state is kept");
+        }
         return fail(MSIM_ERR_OOB, "a device-side index check failed (road or connection index out of range)");
     }
     return MSIM_OK;
@@ -742,6 +807,13 @@ int msim_create(const msim_map* map, const msim_params* params, msim_ctx** out) 
     if (e == cudaSuccess) e = cudaMemsetAsync(c->lookback, 0, sizeof(uint32_t) * kMaxPasses * c->sort_region, c->stream);
     if (e == cudaSuccess) e = cudaMemsetAsync(c->tickets, 0, sizeof(uint32_t) * kMaxPasses, c->stream);
     if (e == cudaSuccess) e = cudaMemsetAsync(c->sort_dirty, 0, sizeof(uint32_t) * kMaxPasses, c->stream);
+    // the index buffers start zeroed (every slot and key in range), so even an index
+    // update that was cut short leaves nothing out of range behind
+    for (int b = 0; b < 2 && e == cudaSuccess; b++) {
+        e = cudaMemsetAsync(c->sk[b], 0, sizeof(uint32_t) * std::max<size_t>(n, 1), c->stream);
+        if (e == cudaSuccess) e = cudaMemsetAsync(c->sv[b], 0, sizeof(uint32_t) * std::max<size_t>(n, 1), c->stream);
+        if (e == cudaSuccess) e = cudaMemsetAsync(c->kstart_b[b], 0, sizeof(uint32_t) * (c->num_keys + 1), c->stream);
+    }
     for (int b = 0; b < 2 && e == cudaSuccess; b++) {
         e = cudaMemsetAsync(c->st[b].pos, 0, sizeof(float2) * std::max<size_t>(n, 1), c->stream);
         if (e == cudaSuccess) e = cudaMemsetAsync(c->st[b].head, 0, sizeof(uint32_t) * std::max<size_t>(n, 1), c->stream);
@@ -845,7 +917,11 @@ int msim_step(msim_ctx* c, uint32_t ticks, uint32_t flags) {
         for (uint32_t t = 0; t < ticks; t++) {
             rc = neighbour_tick(c);
             if (rc != MSIM_OK) {
+                // a launch of the tick failed: the index is rebuilt from scratch by the
+                // next neighbour tick; the move of this tick may or may not have run
                 join_query(c);
+                c->chain_broken = true;
+                reset_index(c);
                 return rc;
             }
             c->tick++;
@@ -857,7 +933,7 @@ int msim_step(msim_ctx* c, uint32_t ticks, uint32_t flags) {
     while (left) {
         uint32_t t = std::min<uint32_t>(left, 256u);
         Prof p(c, K_STEP_MULTI);
-        CK(launch_step(c->stream, step_args(c, t, false)), "k_step_multi");
+        CKL(p, launch_step(c->stream, step_args(c, t, false)), "k_step_multi");
         left -= t;
         c->tick += t;
     }
@@ -1132,6 +1208,52 @@ int msim_get_tick(msim_ctx* c, uint64_t* tick) {
 int msim_get_launch_count(msim_ctx* c, uint64_t* launches) {
     if (!c || !launches) return fail(MSIM_ERR_INVALID, "NULL argument");
     *launches = c->launch_count;
+    return MSIM_OK;
+}
+
+int msim_set_tick_timing(msim_ctx* c, int enable) {
+    int rc = check_ctx(c);
+    if (rc != MSIM_OK) return rc;
+    if (enable) {
+        for (int k = 0; k < 3; k++)
+            if (!c->ev_tick[k]) CK(cudaEventCreate(&c->ev_tick[k]), "cudaEventCreate");
+    }
+    c->tick_timing = enable != 0;
+    c->tick_recorded = false;
+    return MSIM_OK;
+}
+
+int msim_get_tick_times(msim_ctx* c, float* update_ms, float* collision_ms) {
+    int rc = check_ctx(c);
+    if (rc != MSIM_OK) return rc;
+    if (!c->tick_recorded) return fail(MSIM_ERR_INVALID, "no neighbour tick timed since tick timing was enabled");
+    CK(cudaEventSynchronize(c->ev_tick[2]), "cudaEventSynchronize");
+    float u = 0.f, q = 0.f;
+    CK(cudaEventElapsedTime(&u, c->ev_tick[0], c->ev_tick[1]), "cudaEventElapsedTime");
+    CK(cudaEventElapsedTime(&q, c->ev_tick[1], c->ev_tick[2]), "cudaEventElapsedTime");
+    if (update_ms) *update_ms = u;
+    if (collision_ms) *collision_ms = q;
+    return MSIM_OK;
+}
+
+int msim_set_wait_limit(msim_ctx* c, uint32_t polls) {
+    int rc = check_ctx(c);
+    if (rc != MSIM_OK) return rc;
+    c->spin_limit = polls ? polls : kDefaultSpinLimit;
+    return MSIM_OK;
+}
+
+int msim_debug_inject(msim_ctx* c, uint32_t fault, uint32_t arg) {
+    int rc = check_ctx(c);
+    if (rc != MSIM_OK) return rc;
+    if (fault > MSIM_FAULT_LAUNCH) return fail(MSIM_ERR_INVALID, "unknown fault");
+    c->fault = fault;
+    c->fault_arg = arg;
+    return MSIM_OK;
+}
+
+int msim_debug_fail_device_alloc(int64_t after) {
+    g_alloc_budget.store(after < 0 ? -1 : (long long)after);
     return MSIM_OK;
 }
 

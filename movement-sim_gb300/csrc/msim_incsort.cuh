@@ -48,7 +48,7 @@ __global__ __launch_bounds__(kMarkThreads, 5) void k_mark(const uint32_t* __rest
                                                        uint32_t* __restrict__ b_key, uint32_t* __restrict__ b_val,
                                                        uint32_t* hist, unsigned long long* lookback, uint32_t* ticket,
                                                        uint32_t num_tiles, uint32_t* counts, uint32_t* err,
-                                                       unsigned long long* changed_total) {
+                                                       unsigned long long* changed_total, uint32_t spin_limit) {
     constexpr uint32_t FULL = 0xffffffffu;
     constexpr uint32_t NW = kMarkThreads / 32;
     __shared__ uint32_t s_key[kMarkTile], s_val[kMarkTile];  // A entries, then B entries, in q order
@@ -58,10 +58,12 @@ __global__ __launch_bounds__(kMarkThreads, 5) void k_mark(const uint32_t* __rest
     __shared__ uint32_t s_tile, s_pa, s_pb;
     const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     chain_enter();
+    if (index_failed(err)) return;  // an earlier wait gave up: the previous order is incomplete
     if (tid == 0) s_tile = atomicAdd(ticket, 1u);
     for (uint32_t i = tid; i < passes * kRadix; i += kMarkThreads) s_hist[i] = 0u;
     __syncthreads();
     const uint32_t tile = s_tile;
+    if (tile >= num_tiles) return;  // only when the ticket did not start at zero; uniform per block
     const uint32_t base = tile * kMarkTile;
     const uint32_t lt = lanemask_lt();
     // the row ballots go to shared memory (each lane's rank and A/B side come back from
@@ -148,7 +150,7 @@ __global__ __launch_bounds__(kMarkThreads, 5) void k_mark(const uint32_t* __rest
                 const uint32_t first = prefix ? (uint32_t)(__ffs(prefix) - 1) : 32u;
                 const unsigned needed = first == 32u ? FULL : (0xffffffffu >> (31u - first));
                 if (not_ready & needed) {  // a predecessor has not published: poll again
-                    if (++spins > kSpinLimit) {
+                    if (++spins > spin_limit) {
                         if (lane == 0) atomicOr(err, kErrTimeout);
                         break;
                     }
@@ -201,9 +203,11 @@ __global__ __launch_bounds__(kMarkThreads, 5) void k_mark(const uint32_t* __rest
 __global__ __launch_bounds__(256) void k_merge_path(const uint32_t* __restrict__ a_key,
                                                     const uint32_t* __restrict__ b_key,
                                                     const uint32_t* __restrict__ counts, uint32_t n,
-                                                    uint32_t boundaries, uint32_t* __restrict__ split) {
+                                                    uint32_t boundaries, uint32_t* __restrict__ split,
+                                                    const uint32_t* err) {
     constexpr uint32_t FULL = 0xffffffffu;
     chain_enter();
+    if (index_failed(err)) return;
     const uint32_t t = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const uint32_t lane = threadIdx.x & 31;
     if (t >= boundaries) return;  // uniform per warp
@@ -248,6 +252,7 @@ __global__ __launch_bounds__(kMergeThreads, 8) void k_merge(
     __shared__ uint32_t s_outk[kMergeTile], s_outv[kMergeTile];
     __shared__ uint32_t s_prev;  // clamped key of the entry before the tile
     chain_enter();
+    if (index_failed(err)) return;
     const uint32_t tid = threadIdx.x, lane = tid & 31;
     const uint32_t na_all = counts[0], nb_all = counts[1];
     if (na_all + nb_all != n) {  // unreachable unless the split look-back gave up

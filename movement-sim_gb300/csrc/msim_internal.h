@@ -13,6 +13,10 @@ namespace msim {
 void set_error(const std::string& msg);
 int fail(int code, const std::string& msg);
 
+// Every device allocation of the library goes through here: cudaMalloc, or a
+// failure injected by msim_debug_fail_device_alloc.  True on success.
+bool device_malloc(void** p, size_t bytes);
+
 // Owned map (JSON loader, lattice generator).
 struct MapData {
     std::vector<float> road_pos;      // 4 per road

@@ -29,7 +29,8 @@ constexpr uint32_t kFlagAgg = 0x40000000u;
 constexpr uint32_t kFlagPrefix = 0x80000000u;
 constexpr uint32_t kFlagMask = 0xc0000000u;
 constexpr uint32_t kValueMask = 0x3fffffffu;
-constexpr uint32_t kSpinLimit = 1u << 24;  // ~1 s of polling, then give up with kErrTimeout
+// polls of a look-back word before a wait gives up with kErrTimeout: the per-context
+// limit (msim_set_wait_limit) defaults to kDefaultSpinLimit, about a second
 constexpr int kLookBack = 4;               // predecessor tiles read per look-back round of a radix pass
 
 // Kernels of the per-tick chain (move, split, radix passes, merge, key-start fill,
@@ -56,6 +57,14 @@ __device__ __forceinline__ uint32_t ld_relaxed(const uint32_t* p) {
 }
 __device__ __forceinline__ void st_relaxed(uint32_t* p, uint32_t v) {
     asm volatile("st.relaxed.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// After a bounded wait has given up (kErrTimeout in the status word) the index of
+// the tick is incomplete: every later kernel that reads it returns without work
+// (k_permute copies the state in its current order), so no kernel consumes a partial
+// sort until the host has read and cleared the status and rebuilt the index.
+__device__ __forceinline__ bool index_failed(const uint32_t* err) {
+    return err != nullptr && (ld_relaxed(err) & kErrTimeout) != 0u;
 }
 
 // Block-wide exclusive sum over NT threads; s_warp needs NT/32 + 1 words.
@@ -260,7 +269,8 @@ __global__ __launch_bounds__(kSortThreads, 4) void k_onesweep(const uint32_t* __
                                                               uint32_t shift,
                                                               const uint32_t* __restrict__ digit_count,
                                                               uint32_t* lookback, uint32_t* ticket, uint32_t* err,
-                                                              const uint32_t* __restrict__ n_dev, SweepChain chain) {
+                                                              const uint32_t* __restrict__ n_dev, SweepChain chain,
+                                                              uint32_t spin_limit) {
     constexpr int NW = kSortThreads / 32;
     constexpr uint32_t TILE = kSortThreads * ROWS;
     constexpr int G = ROWS < 4 ? ROWS : 4;  // rows whose counter atomics are in flight together
@@ -277,6 +287,7 @@ __global__ __launch_bounds__(kSortThreads, 4) void k_onesweep(const uint32_t* __
 
     const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     chain_enter();
+    if (index_failed(err)) return;  // an earlier wait gave up: the input is incomplete
     if (n_dev) n = min(*n_dev, n);  // item count known only on the device (grid sized for n)
     const uint32_t tiles = n ? (n + TILE - 1u) / TILE : 1u;
     if (chain.next_lookback) {  // clear the next pass's look-back words and ticket
@@ -384,7 +395,7 @@ __global__ __launch_bounds__(kSortThreads, 4) void k_onesweep(const uint32_t* __
             if (done) break;
             j -= take;
             if (take < kLookBack) {
-                if (++spins > kSpinLimit) {
+                if (++spins > spin_limit) {
                     atomicOr(err, kErrTimeout);
                     break;
                 }
@@ -510,11 +521,12 @@ __device__ __noinline__ void list_overflow(const uint32_t* __restrict__ sorted_s
 #include "msim_query.cuh"
 #include "msim_incsort.cuh"
 
-__global__ void k_permute(const uint32_t* __restrict__ ss, EntityState src, EntityState dst, uint32_t n) {
+__global__ void k_permute(const uint32_t* __restrict__ ss, EntityState src, EntityState dst, uint32_t n,
+                          const uint32_t* err) {
     chain_enter();
     const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= n) return;
-    const uint32_t s = ss[p] < n ? ss[p] : p;
+    const uint32_t s = !index_failed(err) && ss[p] < n ? ss[p] : p;
     dst.pos[p] = src.pos[s];
     dst.head[p] = src.head[s];
     dst.rng[p] = src.rng[s];
@@ -686,7 +698,7 @@ cudaError_t launch_step(cudaStream_t s, const StepLaunch& a) {
 cudaError_t launch_onesweep(cudaStream_t s, const uint32_t* keys_in, const uint32_t* vals_in, uint32_t* keys_out,
                             uint32_t* vals_out, uint32_t n, uint32_t shift, const uint32_t* digit_count,
                             uint32_t* lookback, uint32_t* ticket, uint32_t* err, const uint32_t* n_dev,
-                            const SweepChain* chain) {
+                            const SweepChain* chain, uint32_t spin_limit) {
     if (n == 0) return cudaSuccess;
     static bool carveout = false;  // prefer the largest shared-memory carveout: 4 blocks of 43 KB per SM
     if (!carveout) {
@@ -705,10 +717,10 @@ cudaError_t launch_onesweep(cudaStream_t s, const uint32_t* keys_in, const uint3
         const unsigned grid =
             std::min<unsigned>(blocks_for(n, kSortThreads * kSortRowsDev), 4u * (unsigned)(sms > 0 ? sms : 1));
         return launch_chained(k_onesweep<true, kSortRowsDev>, grid, kSortThreads, s, keys_in, vals_in, keys_out,
-                              vals_out, n, shift, digit_count, lookback, ticket, err, n_dev, ch);
+                              vals_out, n, shift, digit_count, lookback, ticket, err, n_dev, ch, spin_limit);
     }
     return launch_chained(k_onesweep<false, kSortRows>, blocks_for(n, kSortTile), kSortThreads, s, keys_in, vals_in,
-                          keys_out, vals_out, n, shift, digit_count, lookback, ticket, err, n_dev, ch);
+                          keys_out, vals_out, n, shift, digit_count, lookback, ticket, err, n_dev, ch, spin_limit);
 }
 
 size_t sort_lookback_words(uint32_t n) {
@@ -729,16 +741,16 @@ uint32_t kstart_chunks(uint64_t num_keys) { return kstart_chunk_cap(num_keys); }
 
 cudaError_t launch_kstart(cudaStream_t s, const uint32_t* sorted_key, uint32_t n, uint32_t* kstart, uint32_t num_keys,
                           uint4* chunks, uint32_t* chunk_count, uint32_t* kernels, const uint32_t* sorted_slot,
-                          const float2* pos, float2* sorted_pos) {
+                          const float2* pos, float2* sorted_pos, const uint32_t* err) {
     if (kernels) *kernels = 0;
     if (num_keys == 0) return cudaSuccess;
     if (kernels) *kernels = 1;
     const uint64_t entries = (uint64_t)num_keys + 1u;
     const bool gather = sorted_slot && pos && sorted_pos && n > 0;
     if ((uint64_t)n > 8u * entries) {  // many positions per key
-        k_kstart_search<<<(unsigned)((entries + 255u) / 256u), 256, 0, s>>>(sorted_key, n, kstart, num_keys);
+        k_kstart_search<<<(unsigned)((entries + 255u) / 256u), 256, 0, s>>>(sorted_key, n, kstart, num_keys, err);
         if (gather) {
-            k_gather_pos<<<blocks_for(n, 256), 256, 0, s>>>(sorted_slot, pos, n, sorted_pos);
+            k_gather_pos<<<blocks_for(n, 256), 256, 0, s>>>(sorted_slot, pos, n, sorted_pos, err);
             if (kernels) *kernels = 2;
         }
     } else if (chunks && chunk_count) {
@@ -746,19 +758,19 @@ cudaError_t launch_kstart(cudaStream_t s, const uint32_t* sorted_key, uint32_t n
         cudaError_t e = cudaMemsetAsync(chunk_count, 0, sizeof(uint32_t), s);
         if (e != cudaSuccess) return e;
         e = launch_chained(k_kstart_pos, blocks_for(n + 1u, 256), 256, s, sorted_key, n, kstart, num_keys, chunks,
-                           chunk_count, cap, sorted_slot, pos, sorted_pos);
+                           chunk_count, cap, sorted_slot, pos, sorted_pos, err);
         if (e != cudaSuccess) return e;
         int dev = 0, sms = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        e = launch_chained(k_kstart_fill, 4u * (sms > 0 ? sms : 1), 256, s, chunks, chunk_count, cap, kstart);
+        e = launch_chained(k_kstart_fill, 4u * (sms > 0 ? sms : 1), 256, s, chunks, chunk_count, cap, kstart, err);
         if (e != cudaSuccess) return e;
         if (kernels) *kernels = 2;
     } else {
         const uint64_t warps = (entries + kKstartWindow - 1u) / kKstartWindow;
-        k_kstart<<<(unsigned)((warps + 7u) / 8u), 256, 0, s>>>(sorted_key, n, kstart, num_keys);
+        k_kstart<<<(unsigned)((warps + 7u) / 8u), 256, 0, s>>>(sorted_key, n, kstart, num_keys, err);
         if (gather) {
-            k_gather_pos<<<blocks_for(n, 256), 256, 0, s>>>(sorted_slot, pos, n, sorted_pos);
+            k_gather_pos<<<blocks_for(n, 256), 256, 0, s>>>(sorted_slot, pos, n, sorted_pos, err);
             if (kernels) *kernels = 2;
         }
     }
@@ -767,7 +779,7 @@ cudaError_t launch_kstart(cudaStream_t s, const uint32_t* sorted_key, uint32_t n
 
 cudaError_t launch_query(cudaStream_t s, uint32_t cap, const uint32_t* kstart, const uint32_t* sorted_slot,
                          const float2* sorted_pos, const uint32_t* slot_id, TileGrid grid, uint32_t n, uint32_t* count,
-                         uint32_t* list, unsigned long long* pair_bins) {
+                         uint32_t* list, unsigned long long* pair_bins, const uint32_t* err) {
     if (n == 0) return cudaSuccess;
     static bool carveout = false;  // 16 blocks of ~9.5 KB per SM
     if (!carveout) {
@@ -780,10 +792,10 @@ cudaError_t launch_query(cudaStream_t s, uint32_t cap, const uint32_t* kstart, c
     }
     if (cap > 0 && list)
         k_query<true><<<blocks_for(n, kQueryThreads), kQueryThreads, 0, s>>>(kstart, sorted_slot, sorted_pos, slot_id,
-                                                                            grid, n, cap, count, list, pair_bins);
+                                                                            grid, n, cap, count, list, pair_bins, err);
     else
         k_query<false><<<blocks_for(n, kQueryThreads), kQueryThreads, 0, s>>>(kstart, sorted_slot, sorted_pos, slot_id,
-                                                                             grid, n, 0u, count, nullptr, pair_bins);
+                                                                             grid, n, 0u, count, nullptr, pair_bins, err);
     return cudaGetLastError();
 }
 
@@ -813,11 +825,11 @@ uint32_t merge_tiles(uint32_t n) { return (n + kMergeTile - 1u) / kMergeTile; }
 cudaError_t launch_mark(cudaStream_t s, const uint32_t* P, bool identity, const uint32_t* PK, const uint32_t* NK,
                         uint32_t n, uint32_t passes, uint32_t* a_key, uint32_t* a_val, uint32_t* b_key,
                         uint32_t* b_val, uint32_t* hist, unsigned long long* lookback, uint32_t* ticket,
-                        uint32_t* counts, uint32_t* err, unsigned long long* changed_total) {
+                        uint32_t* counts, uint32_t* err, unsigned long long* changed_total, uint32_t spin_limit) {
     if (n == 0) return cudaMemsetAsync(counts, 0, 2 * sizeof(uint32_t), s);
     const uint32_t tiles = mark_tiles(n);
     return launch_chained(k_mark, tiles, kMarkThreads, s, P, identity ? 1u : 0u, PK, NK, n, passes, a_key, a_val, b_key,
-                          b_val, hist, lookback, ticket, tiles, counts, err, changed_total);
+                          b_val, hist, lookback, ticket, tiles, counts, err, changed_total, spin_limit);
 }
 
 cudaError_t launch_merge(cudaStream_t s, const uint32_t* a_key, const uint32_t* a_val, const uint32_t* b_key,
@@ -831,7 +843,8 @@ cudaError_t launch_merge(cudaStream_t s, const uint32_t* a_key, const uint32_t* 
     const uint32_t cap = kstart_chunk_cap(num_keys);
     cudaError_t e = cudaMemsetAsync(chunk_count, 0, sizeof(uint32_t), s);  // first: the three kernels chain
     if (e == cudaSuccess)  // a warp per tile boundary
-        e = launch_chained(k_merge_path, (tiles + 1u + 7u) / 8u, 256, s, a_key, b_key, counts, n, tiles + 1u, split);
+        e = launch_chained(k_merge_path, (tiles + 1u + 7u) / 8u, 256, s, a_key, b_key, counts, n, tiles + 1u, split,
+                           static_cast<const uint32_t*>(err));
     if (e == cudaSuccess)
         e = launch_chained(k_merge, tiles, kMergeThreads, s, a_key, a_val, b_key, b_val, counts, split, n, out_key,
                            out_val, pos, sorted_pos, kstart, num_keys, chunks, chunk_count, cap, err);
@@ -839,7 +852,8 @@ cudaError_t launch_merge(cudaStream_t s, const uint32_t* a_key, const uint32_t* 
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    e = launch_chained(k_kstart_fill, 4u * (sms > 0 ? sms : 1), 256, s, chunks, chunk_count, cap, kstart);
+    e = launch_chained(k_kstart_fill, 4u * (sms > 0 ? sms : 1), 256, s, chunks, chunk_count, cap, kstart,
+                       static_cast<const uint32_t*>(err));
     if (e == cudaSuccess && kernels) *kernels = 3;
     return e;
 }
@@ -850,9 +864,10 @@ cudaError_t launch_iota(cudaStream_t s, uint32_t* out, uint32_t n) {
     return cudaGetLastError();
 }
 
-cudaError_t launch_permute(cudaStream_t s, const uint32_t* sorted_slot, EntityState src, EntityState dst, uint32_t n) {
+cudaError_t launch_permute(cudaStream_t s, const uint32_t* sorted_slot, EntityState src, EntityState dst, uint32_t n,
+                           const uint32_t* err) {
     if (n == 0) return cudaSuccess;
-    return launch_chained(k_permute, blocks_for(n, 256), 256, s, sorted_slot, src, dst, n);
+    return launch_chained(k_permute, blocks_for(n, 256), 256, s, sorted_slot, src, dst, n, err);
 }
 
 cudaError_t launch_export_state(cudaStream_t s, EntityState st, uint32_t n, float2* pos, uint32_t* head, uint4* rng,

@@ -67,11 +67,13 @@ struct SweepChain {
 };
 // Look-back words one pass over n items may publish (either tile size).
 size_t sort_lookback_words(uint32_t n);
+// Polls of a look-back word before a wait gives up (kErrTimeout): about a second.
+constexpr uint32_t kDefaultSpinLimit = 1u << 24;
 cudaError_t launch_onesweep(cudaStream_t s, const uint32_t* keys_in, const uint32_t* vals_in,
                             uint32_t* keys_out, uint32_t* vals_out, uint32_t n, uint32_t shift,
                             const uint32_t* digit_count, uint32_t* lookback, uint32_t* ticket,
                             uint32_t* err, const uint32_t* n_dev = nullptr,  // n_dev: count on the device (<= n)
-                            const SweepChain* chain = nullptr);
+                            const SweepChain* chain = nullptr, uint32_t spin_limit = kDefaultSpinLimit);
 cudaError_t launch_ranges(cudaStream_t s, const uint32_t* sorted_key, uint32_t n, uint2* ranges, uint32_t num_keys,
                           uint32_t ybits = 0);
 // Key-start table of sorted keys (num_keys + 1 entries).  chunks / chunk_count
@@ -83,10 +85,11 @@ uint32_t kstart_chunks(uint64_t num_keys);
 cudaError_t launch_kstart(cudaStream_t s, const uint32_t* sorted_key, uint32_t n, uint32_t* kstart, uint32_t num_keys,
                           uint4* chunks = nullptr, uint32_t* chunk_count = nullptr, uint32_t* kernels = nullptr,
                           const uint32_t* sorted_slot = nullptr, const float2* pos = nullptr,
-                          float2* sorted_pos = nullptr);
+                          float2* sorted_pos = nullptr, const uint32_t* err = nullptr);
 cudaError_t launch_query(cudaStream_t s, uint32_t cap, const uint32_t* kstart, const uint32_t* sorted_slot,
                          const float2* sorted_pos, const uint32_t* slot_id, TileGrid grid, uint32_t n, uint32_t* count,
-                         uint32_t* list, unsigned long long* pair_bins);  // pair_bins: kPairBins counters
+                         uint32_t* list, unsigned long long* pair_bins,  // pair_bins: kPairBins counters
+                         const uint32_t* err = nullptr);  // err: the status word (skip after a failed wait)
 // Incremental index update: split the previous sorted order P (keys PK; P[q] = q when
 // identity) by whether the new key NK[slot] changed (A: unchanged, B: changed; counts
 // -> counts[0..1]; B's digit counts -> hist), then, after B is sorted, merge A and B
@@ -98,7 +101,8 @@ uint32_t merge_tiles(uint32_t n);
 cudaError_t launch_mark(cudaStream_t s, const uint32_t* P, bool identity, const uint32_t* PK, const uint32_t* NK,
                         uint32_t n, uint32_t passes, uint32_t* a_key, uint32_t* a_val, uint32_t* b_key,
                         uint32_t* b_val, uint32_t* hist, unsigned long long* lookback, uint32_t* ticket,
-                        uint32_t* counts, uint32_t* err, unsigned long long* changed_total = nullptr);
+                        uint32_t* counts, uint32_t* err, unsigned long long* changed_total = nullptr,
+                        uint32_t spin_limit = kDefaultSpinLimit);
 cudaError_t launch_merge(cudaStream_t s, const uint32_t* a_key, const uint32_t* a_val, const uint32_t* b_key,
                          const uint32_t* b_val, const uint32_t* counts, uint32_t* split, uint32_t n,
                          uint32_t* out_key, uint32_t* out_val, const float2* pos, float2* sorted_pos,
@@ -112,8 +116,9 @@ cudaError_t launch_check_roads(cudaStream_t s, const uint32_t* head, uint32_t n,
 cudaError_t launch_check_roads_range(cudaStream_t s, const uint32_t* head, uint32_t first, uint32_t n,
                                      uint32_t num_roads, uint32_t* first_bad);
 cudaError_t launch_fill(cudaStream_t s, float* out, uint32_t n, float v);
+// With kErrTimeout in *err (may be NULL) the state is copied in its current order.
 cudaError_t launch_permute(cudaStream_t s, const uint32_t* sorted_slot, EntityState src,
-                           EntityState dst, uint32_t n);
+                           EntityState dst, uint32_t n, const uint32_t* err = nullptr);
 cudaError_t launch_export_state(cudaStream_t s, EntityState st, uint32_t n, float2* pos,
                                 uint32_t* head, uint4* rng, float* speed);
 cudaError_t launch_export_neighbours(cudaStream_t s, const uint32_t* sorted_slot, const uint32_t* slot_id,

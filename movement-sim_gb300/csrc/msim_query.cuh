@@ -21,8 +21,10 @@ __device__ __forceinline__ uint32_t clamped_key(const uint32_t* __restrict__ sk,
 // warp writes exactly its window, so no warp fills a long empty stretch of the key
 // space alone.  For key spaces much smaller than n see k_kstart_search.
 __global__ __launch_bounds__(256) void k_kstart(const uint32_t* __restrict__ sk, uint32_t n,
-                                                uint32_t* __restrict__ kstart, uint32_t num_keys) {
+                                                uint32_t* __restrict__ kstart, uint32_t num_keys,
+                                                const uint32_t* err) {
     constexpr uint32_t FULL = 0xffffffffu;
+    if (index_failed(err)) return;
     const uint32_t lane = threadIdx.x & 31;
     const uint64_t b64 = (uint64_t)((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * kKstartWindow;
     if (b64 > num_keys) return;  // uniform per warp
@@ -157,8 +159,10 @@ __global__ __launch_bounds__(256) void k_kstart_pos(const uint32_t* __restrict__
                                                     uint32_t* __restrict__ kstart, uint32_t num_keys,
                                                     uint4* __restrict__ chunks, uint32_t* chunk_count,
                                                     uint32_t chunk_cap, const uint32_t* __restrict__ sv,
-                                                    const float2* __restrict__ pos, float2* __restrict__ sorted_pos) {
+                                                    const float2* __restrict__ pos, float2* __restrict__ sorted_pos,
+                                                    const uint32_t* err) {
     chain_enter();
+    if (index_failed(err)) return;
     const uint32_t lane = threadIdx.x & 31;
     const uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
     if (sorted_pos && q < n) {  // positions in sorted order, for the query's candidate reads
@@ -176,8 +180,9 @@ __global__ __launch_bounds__(256) void k_kstart_pos(const uint32_t* __restrict__
 
 __global__ __launch_bounds__(256) void k_kstart_fill(const uint4* __restrict__ chunks,
                                                      const uint32_t* __restrict__ chunk_count, uint32_t chunk_cap,
-                                                     uint32_t* __restrict__ kstart) {
+                                                     uint32_t* __restrict__ kstart, const uint32_t* err) {
     chain_enter();
+    if (index_failed(err)) return;
     const uint32_t lane = threadIdx.x & 31;
     const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
     const uint32_t count = min(*chunk_count, chunk_cap);
@@ -196,9 +201,10 @@ inline uint32_t kstart_chunk_cap(uint64_t num_keys) {
 // Positions in sorted order (NaN for a slot out of range), for the key-start paths
 // that do not gather them on the way.
 __global__ __launch_bounds__(256) void k_gather_pos(const uint32_t* __restrict__ sv, const float2* __restrict__ pos,
-                                                    uint32_t n, float2* __restrict__ sorted_pos) {
+                                                    uint32_t n, float2* __restrict__ sorted_pos,
+                                                    const uint32_t* err) {
     const uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
-    if (q >= n) return;
+    if (q >= n || index_failed(err)) return;
     const uint32_t slot = sv[q];
     sorted_pos[q] = slot < n ? pos[slot] : make_float2(__int_as_float(0x7fffffff), __int_as_float(0x7fffffff));
 }
@@ -206,9 +212,10 @@ __global__ __launch_bounds__(256) void k_gather_pos(const uint32_t* __restrict__
 // One thread per table entry, binary search over the sorted keys: for key spaces
 // much smaller than the number of positions (many positions per key).
 __global__ __launch_bounds__(256) void k_kstart_search(const uint32_t* __restrict__ sk, uint32_t n,
-                                                       uint32_t* __restrict__ kstart, uint32_t num_keys) {
+                                                       uint32_t* __restrict__ kstart, uint32_t num_keys,
+                                                       const uint32_t* err) {
     const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k > num_keys) return;
+    if (k > num_keys || index_failed(err)) return;
     uint32_t lo = 0, hi = n;  // first position with clamped key >= k
     if (k == num_keys) {
         lo = n;
@@ -342,9 +349,11 @@ __global__ __launch_bounds__(kQueryThreads, 16) void k_query(const uint32_t* __r
                                                          const uint32_t* __restrict__ slot_id, TileGrid g,
                                                          uint32_t n, uint32_t cap, uint32_t* __restrict__ count_out,
                                                          uint32_t* __restrict__ list,
-                                                         unsigned long long* __restrict__ pair_bins) {
+                                                         unsigned long long* __restrict__ pair_bins,
+                                                         const uint32_t* err) {
     constexpr uint32_t FULL = 0xffffffffu;
     __shared__ QueryShared sh;
+    if (index_failed(err)) return;  // uniform per block
     const uint32_t tid = threadIdx.x;
     const uint32_t lane = tid & 31;
     const uint32_t warp = tid >> 5;
@@ -453,9 +462,11 @@ __global__ __launch_bounds__(kQueryThreads, 16) void k_query(const uint32_t* __r
 #pragma unroll
             for (int i = 0; i < kRegKeep; i++) {
                 if ((uint32_t)i >= wmax) continue;  // uniform
-                keep[kRegKeep - 1] = id[i];  // the last slot is free: at most i < kRegKeep are in
+                // keep[0..i) is sorted and slot i is free: insert there and sink it, i
+                // compare-exchanges (w (w - 1) / 2 in all for a warp's largest list w)
+                keep[i] = id[i];
 #pragma unroll
-                for (int j = kRegKeep - 1; j > 0; j--) {
+                for (int j = i; j > 0; j--) {
                     const uint32_t lo = min(keep[j - 1], keep[j]), hi = max(keep[j - 1], keep[j]);
                     keep[j - 1] = lo;
                     keep[j] = hi;

@@ -189,7 +189,8 @@ void Simulator::init() {
     check(msim_create(&view, &p, &ctx_), "msim_create");
     msim_init ini{config_.seed, config_.placement, config_.speed_min, config_.speed_max};
     check(msim_init_entities(ctx_, &ini), "msim_init_entities");
-    check(msim_set_profiling(ctx_, 1), "msim_set_profiling");
+    check(msim_set_tick_timing(ctx_, 1), "msim_set_tick_timing");
+    if (config_.kernel_stats) check(msim_set_profiling(ctx_, 1), "msim_set_profiling");
     auto ents = std::make_shared<std::vector<Entity>>(config_.num_entities);
     check(msim_export_entities_aos(ctx_, ents->data(), ents->size()), "msim_export_entities_aos");
     {
@@ -295,22 +296,12 @@ void Simulator::sim_tick() {  // Simulator.cpp:213-279
     check(msim_sync(ctx_), "msim_sync");
     auto all = std::chrono::steady_clock::now() - t0;
 
-    // device time of the move (k_step, k_permute) and of the index + query kernels
-    double update_ms = 0, total_ms = 0;
-    for (uint32_t k = 0; k < msim_kernel_count(); k++) {
-        uint64_t n = 0;
-        double ms = 0;
-        check(msim_get_kernel_stats(ctx_, k, &n, &ms), "msim_get_kernel_stats");
-        std::string name = msim_kernel_name(k);
-        if (name == "k_export" || name == "k_init") continue;
-        total_ms += ms;
-        if (name == "k_step" || name == "k_permute") update_ms += ms;
-    }
-    double du = update_ms - last_update_ms_, dc = (total_ms - update_ms) - last_collision_ms_;
-    last_update_ms_ = update_ms;
-    last_collision_ms_ = total_ms - update_ms;
-    auto upd = std::chrono::nanoseconds(static_cast<long long>(du * 1e6));
-    auto col = std::chrono::nanoseconds(static_cast<long long>(dc * 1e6));
+    // device time of the update (move, re-ordering) and collision (index + query)
+    // phases of the tick, from the phase events on the context's two streams
+    float update_ms = 0.f, collision_ms = 0.f;
+    check(msim_get_tick_times(ctx_, &update_ms, &collision_ms), "msim_get_tick_times");
+    auto upd = std::chrono::nanoseconds(static_cast<long long>(update_ms * 1e6));
+    auto col = std::chrono::nanoseconds(static_cast<long long>(collision_ms * 1e6));
     update_history_.add_time(upd);
     collision_history_.add_time(col);
     uint64_t tick = 0;

@@ -148,3 +148,73 @@ def test_scale_config_reorders_under_overlap(msim, orc):
             links = _compare(sim, orc, road_map, ost, buf, f"at tick {done}")
             assert links > 0
         assert sim.tick == 135
+
+
+def test_batched_config_512_instances(msim, orc):
+    """The batched ensemble: 512 instances (lattice side U{16..256}, entities
+    log-U[1e3, 2e5], seed = index + 20261203), 1,000 ticks in one graph-captured
+    persistent launch, with the tuner's schedule.  32 instances spread over every
+    size class are compared bit for bit with running each alone (one context, the
+    plain move path), and the largest of them also with the oracle."""
+    sides, ents, seeds = msim.ensemble_config(512, SEED)
+    maps = [msim.RoadMap.lattice(s, sd) for s, sd in zip(sides, seeds)]
+    ticks = 1000
+    order = np.argsort(ents)
+    sample = sorted(set(int(order[k]) for k in np.linspace(0, len(order) - 1, 32).round().astype(int)))
+    with msim.Batch(maps, ents, rng="pcg32", dt=DT) as b:
+        b.init_entities(seeds, placement="fraction", speed=SPEED)
+        b.tune(100)
+        b.init_entities(seeds, placement="fraction", speed=SPEED)
+        b.step(ticks)
+        b.sync()
+        states = {i: b.get_state(i) for i in sample}
+    for i in sample:
+        with msim.Simulation(maps[i], ents[i], rng="pcg32", dt=DT, radius=RADIUS, cap=0) as sim:
+            sim.init_entities(seeds[i], placement="fraction", speed=SPEED)
+            sim.step(ticks)
+            ref = sim.get_state()
+        for k in ("pos", "heading", "rng", "speed"):
+            assert np.array_equal(states[i][k].view(np.uint32), ref[k].view(np.uint32)), (i, ents[i], k)
+    big = max(sample, key=lambda i: ents[i])
+    ost = orc.init_entities(maps[big].road_pos, ents[big], 1, seeds[big], 1, SPEED[0], SPEED[1])
+    _oracle_ticks(orc, maps[big], ost, ticks)
+    assert np.array_equal(states[big]["pos"].view(np.uint32), ost[0].view(np.uint32))
+    assert np.array_equal(states[big]["heading"], ost[1]) and np.array_equal(states[big]["rng"], ost[2])
+
+
+def test_adjoint_config_full_size(msim, orc):
+    """Differentiable calibration at its workload size: 262,144 entities on the
+    128 x 128 lattice, 2,000 ticks, 512 x 512 density grid, checkpoints every 100
+    ticks, target density from hidden road factors U[0.7, 1.3].  Loss, density and
+    both gradients against the FP64 CPU adjoint about the same FP32 trajectory:
+    gradients within 1e-4 relative (norm-wise), loss within 1e-6, density within 1e-5."""
+    torch = pytest.importorskip("torch")
+    import importlib
+
+    cal = importlib.import_module("movement-sim_gb300.calibration")
+    rm = msim.RoadMap.lattice(128, SEED)
+    n, T, grid = 262_144, 2000, (512, 512)
+    calib = cal.Calibration(rm, n, T, dt=DT, rng="pcg32", checkpoint_interval=100, grid=grid, seed=SEED,
+                            placement="fraction", speed=SPEED)
+    with calib:
+        hidden = np.random.default_rng(SEED).uniform(0.7, 1.3, rm.num_roads).astype(np.float32)
+        target = torch.empty(grid[0] * grid[1], dtype=torch.float32, device="cuda")
+        calib.forward(factor=torch.from_numpy(hidden).cuda(), density=target)
+        st = calib.initial_state()
+        speed = torch.from_numpy(st["speed"].copy()).cuda()
+        factor = torch.ones(rm.num_roads, dtype=torch.float32, device="cuda")
+        dens = torch.empty_like(target)
+        loss = calib.forward(speed, factor, target, density=dens)
+        gs = torch.empty(n, dtype=torch.float32, device="cuda")
+        gf = torch.empty(rm.num_roads, dtype=torch.float32, device="cuda")
+        calib.backward(gs, gf)
+        gs64, gf64 = calib.gradients_f64()
+    rl, rdens, rgs, rgf = orc.density_adjoint(rm, st, st["speed"], np.ones(rm.num_roads, np.float32), 1, DT, T, grid,
+                                              target.cpu().numpy(), threads=THREADS)
+    assert abs(loss - rl) <= 1e-6 * abs(rl)
+    np.testing.assert_allclose(dens.cpu().numpy(), rdens, rtol=1e-5, atol=1e-7 * rdens.max())
+    for g, r in ((gs64, rgs), (gf64, rgf)):
+        err = np.linalg.norm(g - r) / np.linalg.norm(r)
+        assert err < 1e-4, err
+    np.testing.assert_array_equal(gs.cpu().numpy(), gs64.astype(np.float32))
+    np.testing.assert_array_equal(gf.cpu().numpy(), gf64.astype(np.float32))

@@ -1,0 +1,146 @@
+"""Failure detection, exercised without faulting the GPU (include/msim_debug.h).
+
+* A bounded device wait that runs out: the look-back chain of the next index update
+  is started at tile 1, so tile 1 waits for a tile 0 that never publishes.  With a
+  short wait limit the kernel gives up, later index kernels skip their work,
+  msim_sync reports MSIM_ERR_TIMEOUT, the entity state is intact, and the next
+  neighbour tick rebuilds the index and matches the oracle again.
+* A kernel launch that reports an error (injected on the host instead of the launch):
+  msim_step returns MSIM_ERR_CUDA, the device is unharmed (msim_sync succeeds), and a
+  caller that sets its state again continues bit-exact with the oracle.
+* Device allocations that fail at every point of context creation: MSIM_ERR_NOMEM,
+  nothing leaked, and creation succeeds once the injection is off.
+
+The reference has no failure detection (its README asks users to turn off the GPU
+hang check), so these have no reference counterpart.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+SEED = 11
+SPEED = (1.0, 1.6)
+
+
+def _oracle(orc, rm, n):
+    return orc.init_entities(rm.road_pos, n, 1, SEED, 1, SPEED[0], SPEED[1])
+
+
+def _advance(orc, rm, ost, ticks):
+    pos, head, rng, speed = ost
+    orc.step(rm.road_pos, rm.road_conn, rm.connections, pos, head, rng, speed, 1, 0.1, ticks, threads=8)
+
+
+def _same_state(sim, ost, what):
+    st = sim.get_state()
+    assert np.array_equal(st["heading"], ost[1]), f"headings differ {what}"
+    assert np.array_equal(st["rng"], ost[2]), f"RNG states differ {what}"
+    assert np.array_equal(st["pos"].view(np.uint32), ost[0].view(np.uint32)), f"positions differ {what}"
+
+
+def _same_neighbours(sim, orc, ost, cap, what):
+    cnt, idx = sim.get_neighbours()
+    ocnt, oidx, opairs = orc.neighbours(ost[0], 2.0, cap, threads=8)
+    assert np.array_equal(cnt, ocnt) and np.array_equal(idx, oidx), f"neighbours differ {what}"
+    assert sim.collision_pairs() == opairs
+
+
+@pytest.mark.parametrize("index", ["full", "auto"])
+def test_wait_timeout_reports_and_recovers(msim, orc, index):
+    """full: the first radix pass of a full sort; auto: the split of an incremental
+    update (both chains have 8 tiles at 30,000 entities)."""
+    rm = msim.RoadMap.lattice(32, 3)
+    n, cap = 30_000, 16
+    ost = _oracle(orc, rm, n)
+    with msim.Simulation(rm, n, rng="pcg32", dt=0.1, radius=2.0, cap=cap, index=index, resort_interval=4) as sim:
+        sim.init_entities(SEED, placement="fraction", speed=SPEED)
+        sim.step(2, neighbours=True)
+        _advance(orc, rm, ost, 2)
+        _same_neighbours(sim, orc, ost, cap, "before the fault")
+        sim.set_wait_limit(2048)
+        sim.inject_fault(msim._capi.FAULT_SORT_TILE)
+        sim.step(1, neighbours=True)
+        with pytest.raises(msim.MsimError) as ei:
+            sim.sync()
+        assert ei.value.code == 4, str(ei.value)  # MSIM_ERR_TIMEOUT
+        _advance(orc, rm, ost, 1)
+        _same_state(sim, ost, "after the timed-out tick")  # the move ran, the state is intact
+        sim.set_wait_limit(0)
+        for t in range(6):  # full sort, then re-ordering and incremental updates again
+            sim.step(1, neighbours=True)
+            _advance(orc, rm, ost, 1)
+            _same_state(sim, ost, f"{t + 1} ticks after recovery")
+            _same_neighbours(sim, orc, ost, cap, f"{t + 1} ticks after recovery")
+        sim.sync()
+
+
+@pytest.mark.parametrize("arg", [0, 1, 2, 4, 7])
+def test_injected_launch_failure(msim, orc, arg):
+    """The (arg+1)-th launch of a 2-tick neighbour step fails on the host; the caller
+    restores its state with msim_set_entities and continues bit-exact."""
+    rm = msim.RoadMap.lattice(32, 4)
+    n, cap = 20_000, 16
+    ost = _oracle(orc, rm, n)
+    with msim.Simulation(rm, n, rng="pcg32", dt=0.1, radius=2.0, cap=cap) as sim:
+        sim.init_entities(SEED, placement="fraction", speed=SPEED)
+        sim.step(1, neighbours=True)
+        _advance(orc, rm, ost, 1)
+        sim.inject_fault(msim._capi.FAULT_LAUNCH, arg)
+        with pytest.raises(msim.MsimError) as ei:
+            sim.step(2, neighbours=True)
+        assert ei.value.code == 3, str(ei.value)  # MSIM_ERR_CUDA
+        sim.sync()  # nothing happened on the device
+        sim.set_entities(ost[0], ost[1], ost[2], ost[3])
+        for t in range(4):
+            sim.step(1, neighbours=True)
+            _advance(orc, rm, ost, 1)
+            _same_state(sim, ost, f"{t + 1} ticks after the failed launch")
+            _same_neighbours(sim, orc, ost, cap, f"{t + 1} ticks after the failed launch")
+        # a move-only step whose launch fails leaves the state as it was
+        sim.inject_fault(msim._capi.FAULT_LAUNCH, 0)
+        with pytest.raises(msim.MsimError):
+            sim.step(5)
+        sim.step(5)
+        _advance(orc, rm, ost, 5)
+        _same_state(sim, ost, "after a failed move-only launch")
+
+
+def test_device_allocation_failure_everywhere(msim):
+    """Creation fails cleanly at each of its device allocations and leaks nothing."""
+    torch = pytest.importorskip("torch")
+    L = msim.lib()
+    rm = msim.RoadMap.lattice(16, 1)
+    msim.Simulation(rm, 5000, radius=2.0, cap=8).close()  # the CUDA context exists from here on
+    torch.cuda.synchronize()
+    free0 = torch.cuda.mem_get_info()[0]
+    failures = 0
+    try:
+        for after in range(0, 400):
+            L.msim_debug_fail_device_alloc(after)
+            try:
+                sim = msim.Simulation(rm, 5000, radius=2.0, cap=8)
+            except msim.MsimError as e:
+                assert e.code == 5, str(e)  # MSIM_ERR_NOMEM
+                failures += 1
+                continue
+            sim.close()
+            break
+        else:
+            raise AssertionError("creation never succeeded")
+        # the batch and the calibration context too
+        for after in (0, 3, 9):
+            L.msim_debug_fail_device_alloc(after)
+            with pytest.raises(msim.MsimError) as ei:
+                msim.Batch([rm, rm], [1000, 2000])
+            assert ei.value.code == 5
+    finally:
+        L.msim_debug_fail_device_alloc(-1)
+    assert failures >= 20  # every allocation point of msim_create was hit
+    torch.cuda.synchronize()
+    free1 = torch.cuda.mem_get_info()[0]
+    assert abs(free0 - free1) < (16 << 20), f"device memory changed by {free0 - free1} bytes"
+    with msim.Simulation(rm, 5000, rng="pcg32", dt=0.1, radius=2.0, cap=8) as sim:
+        sim.init_entities(SEED, placement="fraction", speed=SPEED)
+        sim.step(3, neighbours=True)
+        sim.sync()

@@ -24,8 +24,9 @@ REFERENCE_MAP = _reference_root() / "test_map.json"
 
 
 def test_header_symbols_exported(msim):
-    decls = re.findall(r"^\s*(?:int|void|uint32_t|const char\*)\s+(msim_\w+)\s*\(",
-                       (ROOT / "include" / "msim.h").read_text(), re.M)
+    decls = [d for h in ("msim.h", "msim_debug.h")
+             for d in re.findall(r"^\s*(?:int|void|uint32_t|const char\*)\s+(msim_\w+)\s*\(",
+                                 (ROOT / "include" / h).read_text(), re.M)]
     assert len(decls) >= 30
     lib = msim.lib()
     for name in decls:
