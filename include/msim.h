@@ -202,7 +202,7 @@ int msim_get_neighbours(msim_ctx* ctx, uint32_t* count, uint32_t* idx);
  * Replaces one Simulator::sim_tick (Simulator.cpp:213-279: the move and collision
  * dispatches, then the entity readback of :248-263) for a caller that owns the state
  * on the host and uploads it first (Simulator.cpp:189-193).  The entities go in
- * chunks of at least 65,536 (up to 8): a chunk is moved as soon as it has arrived and
+ * chunks of at least 65,536 (up to 4): a chunk is moved as soon as it has arrived and
  * downloaded while later chunks still upload, so the two copy directions overlap;
  * the index and the query follow once every chunk has moved.  With page-locked host
  * buffers (msim_host_alloc) the copies run asynchronously; pageable ones work too.
@@ -213,8 +213,12 @@ int msim_get_neighbours(msim_ctx* ctx, uint32_t* count, uint32_t* idx);
  * only the headings and RNG states that change (entities at a road end) are written
  * back, by the move kernel through the arrays' device mapping, and just positions
  * and counts are downloaded.  Synchronous.  A heading naming a road out of
- * range gives MSIM_ERR_OOB and keeps the previous state (as msim_set_entities);
- * the outputs are then undefined. */
+ * range gives MSIM_ERR_OOB and keeps the context's previous state (as
+ * msim_set_entities); the outputs are then undefined, and so are the input heading
+ * and rng arrays when they are also the outputs (in place): chunks before the bad
+ * one may already have been moved and their changed headings and RNG states written
+ * back into them.  A caller that may pass bad headings and needs its arrays intact
+ * passes separate output arrays. */
 int msim_tick_host(msim_ctx* ctx, const float* in_pos, const uint32_t* in_heading, const uint32_t* in_rng,
                    const float* in_speed, uint32_t flags, float* out_pos, uint32_t* out_heading,
                    uint32_t* out_rng, uint32_t* out_count, uint32_t* out_idx);
@@ -263,6 +267,16 @@ int msim_quad_tree_build(const float* pos, uint32_t n, float width, float height
 int msim_query_neighbours_noalloc(const float* d_pos, uint32_t n, float world_w, float world_h, float radius,
                                   uint32_t cap, uint32_t* d_count, uint32_t* d_idx, uint32_t* d_status,
                                   void* stream);
+
+/* No counterpart in the reference (its state lives only in the Kompute tensors).
+ * Snapshot of the entity state by entity id (positions, headings, RNG states,
+ * speeds) and the tick counter to a file, and resume from one: msim_load_state
+ * checks that the file was written for the same entity count, map size and RNG,
+ * then sets the state as msim_set_entities does (the next neighbour tick rebuilds
+ * the index) and restores the tick counter.  A run resumed from a snapshot gives
+ * the same results as the run that wrote it.  Synchronous. */
+int msim_save_state(msim_ctx* ctx, const char* path);
+int msim_load_state(msim_ctx* ctx, const char* path);
 
 /* Number of ticks run since msim_create (one tick = move [+ collision]). */
 int msim_get_tick(msim_ctx* ctx, uint64_t* tick);

@@ -294,6 +294,14 @@ class Simulation:
         check(lib().msim_get_launch_count(self._ctx, ctypes.byref(v)))
         return v.value
 
+    def save_state(self, path) -> None:
+        """Snapshot of the entity state and tick counter (msim_save_state)."""
+        check(lib().msim_save_state(self._ctx, str(path).encode()))
+
+    def load_state(self, path) -> None:
+        """Resume from a snapshot written for the same configuration (msim_load_state)."""
+        check(lib().msim_load_state(self._ctx, str(path).encode()))
+
     def set_wait_limit(self, polls: int) -> None:
         """Polls before a bounded device wait of the index gives up (0: the default)."""
         check(lib().msim_set_wait_limit(self._ctx, polls))

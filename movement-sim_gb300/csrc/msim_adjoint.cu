@@ -795,6 +795,7 @@ int msim_adj_get_initial_state(msim_adj* a, float* pos, uint32_t* heading, uint3
 
 int msim_adj_forward(msim_adj* a, const float* d_speed, const float* d_factor, const float* d_target,
                      float* d_density, uint32_t mode, double* loss) {
+    msim::NvtxRange range("msim_adj_forward");
     if (!a) return fail(MSIM_ERR_INVALID, "NULL argument");
     if (mode > 2) return fail(MSIM_ERR_INVALID, "mode must be 0 (natural), 1 (record events) or 2 (replay events)");
     if (mode == 2 && !a->have_sched) return fail(MSIM_ERR_INVALID, "no recorded event schedule to replay");
@@ -834,6 +835,7 @@ int msim_adj_forward(msim_adj* a, const float* d_speed, const float* d_factor, c
 }
 
 int msim_adj_backward(msim_adj* a, float* d_grad_speed, float* d_grad_factor) {
+    msim::NvtxRange range("msim_adj_backward");
     if (!a) return fail(MSIM_ERR_INVALID, "NULL argument");
     if (!a->have_forward) return fail(MSIM_ERR_INVALID, "backward needs a forward first");
     cudaSetDevice(a->device);

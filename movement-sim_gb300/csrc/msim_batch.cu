@@ -462,6 +462,7 @@ int msim_batch_init_entities(msim_batch* b, const msim_init* inits) {
 }
 
 int msim_batch_step(msim_batch* b, uint32_t ticks) {
+    msim::NvtxRange range("msim_batch_step");
     if (!b) return fail(MSIM_ERR_INVALID, "batch is NULL");
     cudaSetDevice(b->device);
     if (ticks == 0 || b->num_items == 0) return MSIM_OK;

@@ -3,6 +3,7 @@
 #include <algorithm>
 #include <atomic>
 #include <cmath>
+#include <cstdio>
 #include <cstring>
 #include <new>
 #include <string>
@@ -506,6 +507,7 @@ int incremental_index(msim_ctx* c) {
 
 // The update itself, for new keys (by slot) already in c->key.
 int incremental_update(msim_ctx* c) {
+    NvtxRange range("msim index update");
     int rc = inject_sort_tile(c, c->mark_ticket);
     if (rc != MSIM_OK) return rc;
     {
@@ -556,6 +558,7 @@ int key_start_table(msim_ctx* c);
 int run_query(msim_ctx* c, bool overlap);
 
 int neighbour_tick(msim_ctx* c) {
+    NvtxRange range("msim neighbour tick");
     int rc;
     if (c->tick_timing) CK(cudaEventRecord(c->ev_tick[0], c->stream), "cudaEventRecord");
     if (c->have_sort && c->since_permute >= c->resort) {
@@ -590,6 +593,7 @@ int key_start_table(msim_ctx* c) {
 
 // The radius query over the index just built.
 int run_query(msim_ctx* c, bool overlap) {
+    NvtxRange range("msim query");
     // The query reads only the index (key-start table, sorted slots and positions)
     // and slot ids: the next tick's move step may overwrite positions meanwhile.  With
     // profiling on everything stays on one stream so the kernel times do not overlap.
@@ -906,6 +910,7 @@ int msim_set_road_factors(msim_ctx* c, const float* factors) {
 }
 
 int msim_step(msim_ctx* c, uint32_t ticks, uint32_t flags) {
+    NvtxRange range("msim_step");
     int rc = check_ctx(c);
     if (rc != MSIM_OK) return rc;
     if (flags & ~MSIM_STEP_NEIGHBOURS) return fail(MSIM_ERR_INVALID, "unknown step flags");
@@ -999,6 +1004,7 @@ int msim_get_neighbours(msim_ctx* c, uint32_t* count, uint32_t* idx) {
 int msim_tick_host(msim_ctx* c, const float* in_pos, const uint32_t* in_heading, const uint32_t* in_rng,
                    const float* in_speed, uint32_t flags, float* out_pos, uint32_t* out_heading, uint32_t* out_rng,
                    uint32_t* out_count, uint32_t* out_idx) {
+    NvtxRange range("msim_tick_host");
     int rc = check_ctx(c);
     if (rc != MSIM_OK) return rc;
     if (flags & ~MSIM_STEP_NEIGHBOURS) return fail(MSIM_ERR_INVALID, "unknown step flags");
@@ -1202,6 +1208,72 @@ int msim_export_quad_tree(msim_ctx* c, uint32_t max_depth, uint32_t node_cap, vo
 int msim_get_tick(msim_ctx* c, uint64_t* tick) {
     if (!c || !tick) return fail(MSIM_ERR_INVALID, "NULL argument");
     *tick = c->tick;
+    return MSIM_OK;
+}
+
+// Snapshot file: "MSIMSNP1", then u32 num_entities, num_roads, num_connections,
+// rng_kind, u64 tick, then by entity id pos (2 f32), heading (u32), rng (4 u32) and
+// speed (f32) arrays, little-endian as the host writes them.
+namespace {
+constexpr char kSnapMagic[8] = {'M', 'S', 'I', 'M', 'S', 'N', 'P', '1'};
+struct SnapHeader {
+    char magic[8];
+    uint32_t n, roads, conns, rng_kind;
+    uint64_t tick;
+};
+}  // namespace
+
+int msim_save_state(msim_ctx* c, const char* path) {
+    int rc = check_ctx(c);
+    if (rc != MSIM_OK) return rc;
+    if (!path) return fail(MSIM_ERR_INVALID, "path is NULL");
+    const size_t n = c->n;
+    std::vector<float> pos(2 * n), speed(n);
+    std::vector<uint32_t> head(n), rng(4 * n);
+    if ((rc = msim_get_state(c, pos.data(), head.data(), rng.data(), speed.data())) != MSIM_OK) return rc;
+    SnapHeader h{};
+    std::memcpy(h.magic, kSnapMagic, sizeof(h.magic));
+    h.n = c->n;
+    h.roads = c->R;
+    h.conns = c->C;
+    h.rng_kind = c->params.rng_kind;
+    h.tick = c->tick;
+    FILE* f = std::fopen(path, "wb");
+    if (!f) return fail(MSIM_ERR_IO, std::string("cannot write ") + path);
+    bool ok = std::fwrite(&h, sizeof(h), 1, f) == 1 && std::fwrite(pos.data(), sizeof(float), 2 * n, f) == 2 * n &&
+              std::fwrite(head.data(), sizeof(uint32_t), n, f) == n &&
+              std::fwrite(rng.data(), sizeof(uint32_t), 4 * n, f) == 4 * n &&
+              std::fwrite(speed.data(), sizeof(float), n, f) == n;
+    ok = (std::fclose(f) == 0) && ok;
+    return ok ? MSIM_OK : fail(MSIM_ERR_IO, std::string("short write to ") + path);
+}
+
+int msim_load_state(msim_ctx* c, const char* path) {
+    int rc = check_ctx(c);
+    if (rc != MSIM_OK) return rc;
+    if (!path) return fail(MSIM_ERR_INVALID, "path is NULL");
+    FILE* f = std::fopen(path, "rb");
+    if (!f) return fail(MSIM_ERR_IO, std::string("cannot read ") + path);
+    SnapHeader h{};
+    if (std::fread(&h, sizeof(h), 1, f) != 1 || std::memcmp(h.magic, kSnapMagic, sizeof(h.magic)) != 0) {
+        std::fclose(f);
+        return fail(MSIM_ERR_INVALID, std::string(path) + " is not a snapshot");
+    }
+    if (h.n != c->n || h.roads != c->R || h.conns != c->C || h.rng_kind != c->params.rng_kind) {
+        std::fclose(f);
+        return fail(MSIM_ERR_INVALID, "snapshot of another configuration (entities, map or RNG differ)");
+    }
+    const size_t n = c->n;
+    std::vector<float> pos(2 * n), speed(n);
+    std::vector<uint32_t> head(n), rng(4 * n);
+    const bool ok = std::fread(pos.data(), sizeof(float), 2 * n, f) == 2 * n &&
+                    std::fread(head.data(), sizeof(uint32_t), n, f) == n &&
+                    std::fread(rng.data(), sizeof(uint32_t), 4 * n, f) == 4 * n &&
+                    std::fread(speed.data(), sizeof(float), n, f) == n;
+    std::fclose(f);
+    if (!ok) return fail(MSIM_ERR_IO, std::string("truncated snapshot ") + path);
+    if ((rc = msim_set_entities(c, pos.data(), head.data(), rng.data(), speed.data())) != MSIM_OK) return rc;
+    c->tick = h.tick;
     return MSIM_OK;
 }
 

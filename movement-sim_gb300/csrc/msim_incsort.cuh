@@ -239,7 +239,7 @@ __global__ __launch_bounds__(256) void k_merge_path(const uint32_t* __restrict__
 // Merges tile t of the output: A entries [split[t], split[t+1]) and the matching B
 // entries, in shared memory (ranks by binary search in the other segment), then
 // writes the sorted keys and slots, the positions in sorted order and the key-start
-// entries owned by each position (fill_key_gaps).
+// entries owned by each thread's consecutive positions (one walk per thread, fill_run).
 // 8 blocks per SM (32 registers): 0.158 ms at 16 M against 0.173 at the 40 registers
 // the compiler picks alone (6 blocks).
 __global__ __launch_bounds__(kMergeThreads, 8) void k_merge(
@@ -253,7 +253,7 @@ __global__ __launch_bounds__(kMergeThreads, 8) void k_merge(
     __shared__ uint32_t s_prev;  // clamped key of the entry before the tile
     chain_enter();
     if (index_failed(err)) return;
-    const uint32_t tid = threadIdx.x, lane = tid & 31;
+    const uint32_t tid = threadIdx.x;
     const uint32_t na_all = counts[0], nb_all = counts[1];
     if (na_all + nb_all != n) {  // unreachable unless the split look-back gave up
         if (tid == 0) atomicOr(err, kErrOob);
@@ -342,32 +342,40 @@ __global__ __launch_bounds__(kMergeThreads, 8) void k_merge(
         gp[k] = slot < n ? pos[slot] : make_float2(__int_as_float(0x7fffffff), __int_as_float(0x7fffffff));
     }
 #pragma unroll
-    for (uint32_t k = 0; k < kPer; k++) {
+    for (uint32_t k = 0; k < kPer; k++) {  // sorted keys, slots and positions: coalesced rows
         const uint32_t i = k * kMergeThreads + tid;
-        const bool ok = i < cnt;
-        uint32_t from = 0, len = 0;
-        const uint32_t p = d0 + i;
-        if (ok) {
-            const uint32_t key = s_outk[i], slot = s_outv[i];
-            out_key[p] = key;
-            out_val[p] = slot;
+        if (i < cnt) {
+            const uint32_t p = d0 + i;
+            out_key[p] = s_outk[i];
+            out_val[p] = s_outv[i];
             sorted_pos[p] = gp[k];
-            const uint32_t kc = key < num_keys ? key : num_keys - 1u;
-            uint32_t kp = i > 0 ? s_outk[i - 1u] : prev_tile;
-            if (i > 0) kp = kp < num_keys ? kp : num_keys - 1u;
-            from = p == 0 ? 0u : kp + 1u;  // position p owns the entries (key[p-1], key[p]]
-            len = kc >= from ? kc - from + 1u : 0u;
         }
-        fill_key_gaps(from, len, p, lane, kstart, chunks, chunk_count, chunk_cap);
     }
-    if (d1 == n) {  // the tail (key[n-1], num_keys] belongs to n
-        uint32_t from = 0, len = 0;
-        if (tid == 0) {
-            const uint32_t kl = s_outk[cnt - 1u];
-            const uint32_t kc = kl < num_keys ? kl : num_keys - 1u;
-            from = kc + 1u;
-            len = num_keys + 1u - from;
+    // Key-start entries: position p owns the entries (key[p-1], key[p]], so the kPer
+    // consecutive positions [tid * kPer, tid * kPer + kPer) of a thread own one
+    // contiguous stretch of the table, written in one walk (about kPer entries at
+    // the workloads' densities; a walk costs a few instructions per entry where a
+    // per-position fill ran a warp-wide loop to the longest gap of each row).  Gaps
+    // longer than kGapWarp entries go to the chunk list (k_kstart_fill).
+    const uint32_t i0 = tid * kPer;
+    if (i0 < cnt) {
+        const uint32_t kp = i0 ? s_outk[i0 - 1u] : prev_tile;
+        uint32_t e = d0 + i0 == 0 ? 0u : (kp < num_keys ? kp : num_keys - 1u) + 1u;  // first entry not yet owned
+#pragma unroll
+        for (uint32_t k = 0; k < kPer; k++) {
+            const uint32_t i = i0 + k;
+            if (i >= cnt) break;
+            const uint32_t key = s_outk[i];
+            const uint32_t kc = key < num_keys ? key : num_keys - 1u;
+            if (kc >= e) {
+                fill_run(e, kc - e + 1u, d0 + i, kstart, chunks, chunk_count, chunk_cap);
+                e = kc + 1u;
+            }
         }
-        fill_key_gaps(from, len, n, lane, kstart, chunks, chunk_count, chunk_cap);
+    }
+    if (d1 == n && tid == 0) {  // the tail (key[n-1], num_keys] belongs to n
+        const uint32_t kl = s_outk[cnt - 1u];
+        const uint32_t from = (kl < num_keys ? kl : num_keys - 1u) + 1u;
+        fill_run(from, num_keys + 1u - from, n, kstart, chunks, chunk_count, chunk_cap);
     }
 }

@@ -5,9 +5,21 @@
 #include <string>
 #include <vector>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "msim.h"
 
 namespace msim {
+
+// NVTX range over a host scope (the per-tick phases show up by name in Nsight
+// timelines; with no tool attached a push/pop is a pointer check).  The reference's
+// counterpart is its RenderDoc capture around one tick (Simulator.cpp:403-450).
+struct NvtxRange {
+    explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+    ~NvtxRange() { nvtxRangePop(); }
+    NvtxRange(const NvtxRange&) = delete;
+    NvtxRange& operator=(const NvtxRange&) = delete;
+};
 
 // Thread-local error text behind msim_last_error().
 void set_error(const std::string& msg);

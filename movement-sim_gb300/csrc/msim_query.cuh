@@ -155,6 +155,26 @@ __device__ __forceinline__ void fill_key_gaps(uint32_t from, uint32_t len, uint3
     }
 }
 
+// Writes kstart[from + r] = value for r < len by one thread: directly up to kGapWarp
+// entries, in kGapChunk-entry chunks appended to the list beyond that.
+__device__ __forceinline__ void fill_run(uint32_t from, uint32_t len, uint32_t value, uint32_t* __restrict__ kstart,
+                                         uint4* __restrict__ chunks, uint32_t* chunk_count, uint32_t chunk_cap) {
+    if (len <= kGapWarp) {
+        for (uint32_t r = 0; r < len; r++) kstart[from + r] = value;
+        return;
+    }
+    const uint32_t m = (len + kGapChunk - 1u) / kGapChunk;
+    const uint32_t base = atomicAdd(chunk_count, m);
+    if (base + m > chunk_cap) {  // unreachable: chunk_cap bounds every key space; stay correct anyway
+        for (uint32_t r = 0; r < len; r++) kstart[from + r] = value;
+        return;
+    }
+    for (uint32_t c = 0; c < m; c++) {
+        const uint32_t off = c * kGapChunk;
+        chunks[base + c] = make_uint4(from + off, len - off < kGapChunk ? len - off : kGapChunk, value, 0u);
+    }
+}
+
 __global__ __launch_bounds__(256) void k_kstart_pos(const uint32_t* __restrict__ sk, uint32_t n,
                                                     uint32_t* __restrict__ kstart, uint32_t num_keys,
                                                     uint4* __restrict__ chunks, uint32_t* chunk_count,
@@ -473,10 +493,12 @@ __global__ __launch_bounds__(kQueryThreads, 16) void k_query(const uint32_t* __r
                 }
             }
 #pragma unroll
-            for (int i = 0; i < kRegKeep; i++)
+            for (int i = 0; i < kRegKeep; i++) {
+                if ((uint32_t)i >= wmax) break;  // uniform
                 if ((uint32_t)i < kept) out[i] = keep[i];
+            }
         } else {
-            list_overflow(sorted_slot, sorted_pos, slot_id, kstart, g, n, p, me, x0, x1, y0, y1, cap, out);
+            list_overflow(sorted_slot, sorted_pos, slot_id, kstart, g, n, p, cap, out);
         }
     }
 }

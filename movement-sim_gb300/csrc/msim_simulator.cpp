@@ -3,6 +3,8 @@
 // dispatches per tick become one msim_step(ctx, 1, MSIM_STEP_NEIGHBOURS).
 #include "msim_simulator.hpp"
 
+#include "msim_internal.h"
+
 #include <cstdio>
 #include <ctime>
 #include <iostream>
@@ -291,6 +293,7 @@ uint64_t Simulator::get_collision_pairs() const {
 }
 
 void Simulator::sim_tick() {  // Simulator.cpp:213-279
+    msim::NvtxRange range("sim::Simulator::sim_tick");
     auto t0 = std::chrono::steady_clock::now();
     check(msim_step(ctx_, 1, MSIM_STEP_NEIGHBOURS), "msim_step");
     check(msim_sync(ctx_), "msim_sync");
