@@ -75,9 +75,9 @@ KERNEL_BYTES = {
 # one ncu capture of the same workload at full size (third neighbour tick; 1-pass
 # metrics; profiles/scale_16M_dram_traffic.md); scaled by the entities of the run
 # warp instructions per entity-step of k_batch_step: smsp__inst_executed.sum of one
-# ncu capture (397.6 M for 64 instances, 2,058,939 entities, 100 ticks, tuned
+# ncu capture (405.8 M for 64 instances, 2,058,939 entities, 100 ticks, tuned
 # schedule; profiles/batched_64_instances_k_batch_step_issue.md) over entities x ticks
-NCU_BATCH_WARP_INSTR_PER_ENTITY_STEP = 1.931
+NCU_BATCH_WARP_INSTR_PER_ENTITY_STEP = 1.971
 
 NCU_DRAM_BYTES_PER_ENTITY = {
     "scale": {"k_query": 26.87, "k_merge": 32.78, "k_mark": 16.91, "k_step": 27.98},

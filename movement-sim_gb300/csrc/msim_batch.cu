@@ -104,7 +104,11 @@ __device__ __forceinline__ void run_tile(const BatchArgs& a, const DeviceMap& m,
     }
 }
 
-template <int RNG>
+// EMAX: the largest entities-per-thread count of the schedule.  Each value is its own
+// kernel, so a schedule of one entity per thread does not pay the registers of the
+// four-entity path (72 registers and 43 % of the warps resident with all three paths
+// in one kernel).
+template <int RNG, int EMAX>
 __global__ void k_batch_step(BatchArgs a) {
     __shared__ uint32_t s_item;
     while (true) {
@@ -122,8 +126,8 @@ __global__ void k_batch_step(BatchArgs a) {
         m.factor = nullptr;
         m.num_roads = d.num_roads;
         m.num_conn = d.num_conn;
-        if (it.ept == 4) run_tile<RNG, 4>(a, m, it);
-        else if (it.ept == 2) run_tile<RNG, 2>(a, m, it);
+        if (EMAX >= 4 && it.ept == 4) run_tile<RNG, 4>(a, m, it);
+        else if (EMAX >= 2 && it.ept == 2) run_tile<RNG, 2>(a, m, it);
         else run_tile<RNG, 1>(a, m, it);
     }
 }
@@ -256,12 +260,19 @@ int upload_items(msim_batch* b, const std::vector<WorkItem>& items) {
     return MSIM_OK;
 }
 
+// The kernel instantiation for a schedule: RNG and its largest entities per thread.
+using BatchKernel = void (*)(BatchArgs);
+BatchKernel batch_kernel(uint32_t rng_kind, const msim_batch_schedule& s) {
+    uint32_t emax = 1;
+    for (uint32_t c = 0; c < s.num_classes && c < MSIM_BATCH_MAX_CLASSES; c++)
+        emax = std::max(emax, s.entities_per_thread[c]);
+    if (rng_kind == 1) return emax >= 4 ? k_batch_step<1, 4> : emax == 2 ? k_batch_step<1, 2> : k_batch_step<1, 1>;
+    return emax >= 4 ? k_batch_step<0, 4> : emax == 2 ? k_batch_step<0, 2> : k_batch_step<0, 1>;
+}
+
 int occupancy(msim_batch* b, uint32_t threads) {
     int per_sm = 0;
-    if (b->rng_kind == 1)
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch_step<1>, (int)threads, 0);
-    else
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch_step<0>, (int)threads, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batch_kernel(b->rng_kind, b->sched), (int)threads, 0);
     return std::max(per_sm, 1);
 }
 
@@ -290,10 +301,7 @@ cudaError_t enqueue(msim_batch* b, uint32_t ticks) {
     const uint32_t threads = b->sched.block_threads;
     const int grid = b->sms * occupancy(b, threads);
     BatchArgs a = args_of(b, ticks);
-    if (b->rng_kind == 1)
-        k_batch_step<1><<<grid, threads, 0, b->stream>>>(a);
-    else
-        k_batch_step<0><<<grid, threads, 0, b->stream>>>(a);
+    batch_kernel(b->rng_kind, b->sched)<<<grid, threads, 0, b->stream>>>(a);
     return cudaGetLastError();
 }
 
