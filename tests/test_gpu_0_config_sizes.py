@@ -218,3 +218,47 @@ def test_adjoint_config_full_size(msim, orc):
         assert err < 1e-4, err
     np.testing.assert_array_equal(gs.cpu().numpy(), gs64.astype(np.float32))
     np.testing.assert_array_equal(gf.cpu().numpy(), gf64.astype(np.float32))
+
+
+@pytest.mark.parametrize("n,side,ticks,with_idx", [(16_000_000, 1024, 4, False), (1_000_000, 256, 20, True)])
+def test_host_tick_config_sizes(msim, orc, n, side, ticks, with_idx):
+    """The end-to-end path the benchmark times: msim_tick_host in place (the same
+    page-locked arrays for input and output; only positions and counts downloaded,
+    the changed headings and RNG states written into the arrays by the move kernel).
+    16 M entities: 4 host ticks, state and counts against the oracle after each; 1 M:
+    20 host ticks, with the id lists too."""
+    if n > 4_000_000:
+        avail = _host_available_bytes()
+        if avail is not None and avail < n * 200:
+            pytest.skip(f"host memory: {avail >> 30} GiB available")
+    road_map = msim.RoadMap.lattice(side, SEED)
+    with msim.Simulation(road_map, n, rng="pcg32", dt=DT, radius=RADIUS, cap=CAP) as sim:
+        sim.init_entities(SEED, placement="fraction", speed=SPEED)
+        st = sim.get_state()
+        bufs = {"pos": msim.PinnedBuffer((n, 2), np.float32), "heading": msim.PinnedBuffer(n, np.uint32),
+                "rng": msim.PinnedBuffer((n, 4), np.uint32), "count": msim.PinnedBuffer(n, np.uint32)}
+        if with_idx:
+            bufs["idx"] = msim.PinnedBuffer((n, CAP), np.uint32)
+        try:
+            state = {k: b.array for k, b in bufs.items()}
+            for k in ("pos", "heading", "rng"):
+                state[k][...] = st[k]
+            state["speed"] = st["speed"]
+            ost = (st["pos"].copy(), st["heading"].copy(), st["rng"].copy(), st["speed"].copy())
+            ocnt, oidx = np.empty(n, np.uint32), np.empty((n, CAP), np.uint32) if with_idx else None
+            for t in range(ticks):
+                sim.tick_host(state, neighbours=True, out=state)
+                _oracle_ticks(orc, road_map, ost, 1)
+                what = f"after host tick {t + 1}"
+                assert np.array_equal(state["heading"], ost[1]), f"headings differ {what}"
+                assert np.array_equal(state["rng"], ost[2]), f"RNG states differ {what}"
+                assert np.array_equal(state["pos"].view(np.uint32), ost[0].view(np.uint32)), f"positions differ {what}"
+                c, i, _ = orc.neighbours(ost[0], RADIUS, CAP if with_idx else 0, threads=THREADS, with_idx=with_idx,
+                                         out=(ocnt, oidx))
+                assert np.array_equal(state["count"], c), f"counts differ {what}"
+                if with_idx:
+                    assert np.array_equal(state["idx"], i), f"neighbour lists differ {what}"
+            assert sim.tick == ticks
+        finally:
+            for b in bufs.values():
+                b.free()
