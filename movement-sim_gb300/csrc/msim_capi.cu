@@ -555,7 +555,7 @@ int incremental_update(msim_ctx* c) {
 }
 
 int key_start_table(msim_ctx* c);
-int run_query(msim_ctx* c, bool overlap);
+int run_query(msim_ctx* c, bool overlap, uint32_t* count_by_id = nullptr);
 
 int neighbour_tick(msim_ctx* c) {
     NvtxRange range("msim neighbour tick");
@@ -592,7 +592,8 @@ int key_start_table(msim_ctx* c) {
 }
 
 // The radius query over the index just built.
-int run_query(msim_ctx* c, bool overlap) {
+// count_by_id (only with slots holding their own entity): the counts also by id.
+int run_query(msim_ctx* c, bool overlap, uint32_t* count_by_id) {
     NvtxRange range("msim query");
     // The query reads only the index (key-start table, sorted slots and positions)
     // and slot ids: the next tick's move step may overwrite positions meanwhile.  With
@@ -609,7 +610,8 @@ int run_query(msim_ctx* c, bool overlap) {
         // slots that hold their own entity need no id lookup
         CKL(p, launch_query(qs, c->params.cap, c->kstart, c->sorted_slot, c->sorted_pos,
                         c->slots_identity ? nullptr : cur_state(c).slot_id, c->grid,
-                        c->n, c->nbr_count, c->nbr_list, c->pairs, c->err),
+                        c->n, c->nbr_count, c->nbr_list, c->pairs, c->err,
+                        c->slots_identity ? count_by_id : nullptr),
            "k_query");
     }
     if (qs != c->stream) {
@@ -1122,15 +1124,20 @@ int msim_tick_host(msim_ctx* c, const float* in_pos, const uint32_t* in_heading,
         if (nbr && ((rc = sort_keys(c)) != MSIM_OK || (rc = key_start_table(c)) != MSIM_OK)) return rc;
     }
     if (nbr) {
-        if ((rc = run_query(c, false)) != MSIM_OK) return rc;
+        const bool want_idx = out_idx && c->params.cap;
+        const size_t cap = c->params.cap;
+        uint32_t* d_count = nullptr;
         if (out_count || out_idx) {
-            const bool want_idx = out_idx && c->params.cap;
-            const size_t cap = c->params.cap;
             if ((rc = ensure_stage(c, (size_t)n * sizeof(uint32_t) * (1 + (want_idx ? cap : 0)))) != MSIM_OK)
                 return rc;
-            uint32_t* d_count = static_cast<uint32_t*>(c->stage);
+            d_count = static_cast<uint32_t*>(c->stage);
+        }
+        // slots hold entity ids here: the query writes the counts by id itself, so with
+        // counts alone no export pass runs between the query and their download
+        if ((rc = run_query(c, false, d_count)) != MSIM_OK) return rc;
+        if (out_count || out_idx) {
             uint32_t* d_idx = want_idx ? d_count + n : nullptr;
-            {
+            if (want_idx) {
                 Prof p(c, K_EXPORT);
                 CK(launch_export_neighbours(c->stream, c->sorted_slot, nullptr, c->nbr_count, c->nbr_list, n,
                                             c->params.cap, d_count, d_idx),

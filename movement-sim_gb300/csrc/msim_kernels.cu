@@ -816,7 +816,7 @@ cudaError_t launch_kstart(cudaStream_t s, const uint32_t* sorted_key, uint32_t n
 
 cudaError_t launch_query(cudaStream_t s, uint32_t cap, const uint32_t* kstart, const uint32_t* sorted_slot,
                          const float2* sorted_pos, const uint32_t* slot_id, TileGrid grid, uint32_t n, uint32_t* count,
-                         uint32_t* list, unsigned long long* pair_bins, const uint32_t* err) {
+                         uint32_t* list, unsigned long long* pair_bins, const uint32_t* err, uint32_t* count_by_id) {
     if (n == 0) return cudaSuccess;
     static bool carveout = false;  // 16 blocks of ~9.5 KB per SM
     if (!carveout) {
@@ -829,10 +829,12 @@ cudaError_t launch_query(cudaStream_t s, uint32_t cap, const uint32_t* kstart, c
     }
     if (cap > 0 && list)
         k_query<true><<<blocks_for(n, kQueryThreads), kQueryThreads, 0, s>>>(kstart, sorted_slot, sorted_pos, slot_id,
-                                                                            grid, n, cap, count, list, pair_bins, err);
+                                                                            grid, n, cap, count, list, pair_bins, err,
+                                                                            count_by_id);
     else
         k_query<false><<<blocks_for(n, kQueryThreads), kQueryThreads, 0, s>>>(kstart, sorted_slot, sorted_pos, slot_id,
-                                                                             grid, n, 0u, count, nullptr, pair_bins, err);
+                                                                             grid, n, 0u, count, nullptr, pair_bins, err,
+                                                                             count_by_id);
     return cudaGetLastError();
 }
 

@@ -90,7 +90,10 @@ cudaError_t launch_kstart(cudaStream_t s, const uint32_t* sorted_key, uint32_t n
 cudaError_t launch_query(cudaStream_t s, uint32_t cap, const uint32_t* kstart, const uint32_t* sorted_slot,
                          const float2* sorted_pos, const uint32_t* slot_id, TileGrid grid, uint32_t n, uint32_t* count,
                          uint32_t* list, unsigned long long* pair_bins,  // pair_bins: kPairBins counters
-                         const uint32_t* err = nullptr);  // err: the status word (skip after a failed wait)
+                         const uint32_t* err = nullptr,  // err: the status word (skip after a failed wait)
+                         // count_by_id (may be NULL; only when slot = entity id): every count also
+                         // written at its entity's id
+                         uint32_t* count_by_id = nullptr);
 // Incremental index update: split the previous sorted order P (keys PK; P[q] = q when
 // identity) by whether the new key NK[slot] changed (A: unchanged, B: changed; counts
 // -> counts[0..1]; B's digit counts -> hist), then, after B is sorted, merge A and B

@@ -370,7 +370,7 @@ __global__ __launch_bounds__(kQueryThreads, 16) void k_query(const uint32_t* __r
                                                          uint32_t n, uint32_t cap, uint32_t* __restrict__ count_out,
                                                          uint32_t* __restrict__ list,
                                                          unsigned long long* __restrict__ pair_bins,
-                                                         const uint32_t* err) {
+                                                         const uint32_t* err, uint32_t* __restrict__ count_by_id) {
     constexpr uint32_t FULL = 0xffffffffu;
     __shared__ QueryShared sh;
     if (index_failed(err)) return;  // uniform per block
@@ -452,7 +452,12 @@ __global__ __launch_bounds__(kQueryThreads, 16) void k_query(const uint32_t* __r
     }
     __syncwarp();
     const uint32_t count = valid ? sh.cnt[tid] : 0u;
-    if (valid) count_out[p] = count;
+    if (valid) {
+        count_out[p] = count;
+        // slots that hold their own entity: the count also goes straight to its id's
+        // place (the host tick downloads these, with no export pass after the query)
+        if (count_by_id) count_by_id[sorted_slot[p]] = count;
+    }
     const uint32_t warp_sum = __reduce_add_sync(FULL, count);  // every pair is seen from both ends
     if (lane == 0 && warp_sum) atomicAdd(&pair_bins[(p >> 5) & (kPairBins - 1u)], (unsigned long long)warp_sum);
     if (LIST) {
