@@ -114,6 +114,7 @@ struct msim_ctx {
     // incremental index update: the previous order split into unchanged (a) and
     // changed (b, sorted in place with ping-pong) keys, then merged
     bool order_identity = false;  // sorted_slot[q] == q (right after a re-ordering)
+    bool chunk_count_zeroed = false;  // the move step of this tick zeroed the merge's long-gap counter
     bool slots_identity = false;  // slot s holds entity s (state set from the host, not re-ordered since)
     bool incremental = true;      // index updates from the previous order (else full sorts)
     uint32_t* a_key = nullptr;
@@ -493,13 +494,18 @@ int clear_update_scratch(msim_ctx* c) {
 }
 
 int incremental_index(msim_ctx* c) {
-    int rc = clear_update_scratch(c);
-    if (rc != MSIM_OK) return rc;
+    c->chunk_count_zeroed = false;
     {
         Prof p(c, K_STEP);
         StepLaunch a = step_args(c, 1, true);
         a.hist = nullptr;  // the changed keys' digits are counted by k_mark
+        // the move step clears the update's scratch and the long-gap counter of the index
+        // set the merge will write (no memsets between the chained launches)
+        a.zero_a = c->hist;
+        a.zero_a_words = (uint32_t)c->update_words;
+        a.zero_b = c->kstart_chunk_count_b[c->sorted_key == c->sk[0] ? 1 : 0];
         CKL(p, launch_step(c->stream, a), "k_step");
+        c->chunk_count_zeroed = true;
     }
     if (c->tick_timing) CK(cudaEventRecord(c->ev_tick[1], c->stream), "cudaEventRecord");
     return incremental_update(c);
@@ -543,8 +549,9 @@ int incremental_update(msim_ctx* c) {
         CKL(p, launch_merge(c->stream, c->a_key, c->a_val, c->b_key[c->passes & 1], c->b_val[c->passes & 1],
                         c->ab_counts, c->merge_split, c->n, c->sk[out], c->sv[out], cur_state(c).pos, c->sorted_pos,
                         c->kstart, (uint32_t)c->num_keys, c->kstart_chunks, c->kstart_chunk_count, c->err,
-                        &launched),
+                        &launched, c->chunk_count_zeroed),
            "k_merge");
+        c->chunk_count_zeroed = false;
         if (launched > 1) c->launch_count += launched - 1;
     }
     c->sorted_key = c->sk[out];

@@ -201,6 +201,8 @@ __global__ __launch_bounds__(kStepThreads) void k_step(StepLaunch a) {
     chain_enter();
     const uint32_t lane = threadIdx.x & 31;
     const uint32_t stride = gridDim.x * kStepThreads;
+    for (uint32_t i = blockIdx.x * kStepThreads + threadIdx.x; i < a.zero_a_words; i += stride) a.zero_a[i] = 0u;
+    if (a.zero_b && blockIdx.x == 0 && threadIdx.x == 0) *a.zero_b = 0u;
     for (uint32_t base = blockIdx.x * kStepThreads; base < a.n; base += 2u * stride) {
         uint32_t sl[2];
         bool valid[2];
@@ -875,12 +877,14 @@ cudaError_t launch_merge(cudaStream_t s, const uint32_t* a_key, const uint32_t* 
                          const uint32_t* b_val, const uint32_t* counts, uint32_t* split, uint32_t n,
                          uint32_t* out_key, uint32_t* out_val, const float2* pos, float2* sorted_pos,
                          uint32_t* kstart, uint32_t num_keys, uint4* chunks, uint32_t* chunk_count, uint32_t* err,
-                         uint32_t* kernels) {
+                         uint32_t* kernels, bool chunk_count_zeroed) {
     if (kernels) *kernels = 0;
     if (n == 0 || num_keys == 0) return cudaSuccess;
     const uint32_t tiles = merge_tiles(n);
     const uint32_t cap = kstart_chunk_cap(num_keys);
-    cudaError_t e = cudaMemsetAsync(chunk_count, 0, sizeof(uint32_t), s);  // first: the three kernels chain
+    cudaError_t e = cudaSuccess;
+    if (!chunk_count_zeroed)  // first: the three kernels chain
+        e = cudaMemsetAsync(chunk_count, 0, sizeof(uint32_t), s);
     if (e == cudaSuccess)  // a warp per tile boundary
         e = launch_chained(k_merge_path, (tiles + 1u + 7u) / 8u, 256, s, a_key, b_key, counts, n, tiles + 1u, split,
                            static_cast<const uint32_t*>(err));

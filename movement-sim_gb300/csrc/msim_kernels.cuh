@@ -50,6 +50,12 @@ struct StepLaunch {
     uint32_t* host_head = nullptr;
     uint4* host_rng = nullptr;
     uint32_t id_base = 0;
+    // Words the move step zeroes before its entities (nullptr / 0: none): the next
+    // kernels' scratch, cleared here instead of by memsets that would sit between the
+    // chained launches of the tick.
+    uint32_t* zero_a = nullptr;
+    uint32_t zero_a_words = 0;
+    uint32_t* zero_b = nullptr;  // one word
 };
 
 cudaError_t launch_init_entities(cudaStream_t s, const DeviceMap& m, EntityState st, uint32_t n,
@@ -107,11 +113,13 @@ cudaError_t launch_mark(cudaStream_t s, const uint32_t* P, bool identity, const 
                         uint32_t* b_val, uint32_t* hist, unsigned long long* lookback, uint32_t* ticket,
                         uint32_t* counts, uint32_t* err, unsigned long long* changed_total = nullptr,
                         uint32_t spin_limit = kDefaultSpinLimit);
+// chunk_count_zeroed: the long-gap counter was already zeroed in the tick (else a
+// memset does it first).
 cudaError_t launch_merge(cudaStream_t s, const uint32_t* a_key, const uint32_t* a_val, const uint32_t* b_key,
                          const uint32_t* b_val, const uint32_t* counts, uint32_t* split, uint32_t n,
                          uint32_t* out_key, uint32_t* out_val, const float2* pos, float2* sorted_pos,
                          uint32_t* kstart, uint32_t num_keys, uint4* chunks, uint32_t* chunk_count, uint32_t* err,
-                         uint32_t* kernels);
+                         uint32_t* kernels, bool chunk_count_zeroed = false);
 cudaError_t launch_iota(cudaStream_t s, uint32_t* out, uint32_t n);
 // *first_bad = first i with (head[i] & road mask) >= num_roads, or 0xffffffff
 cudaError_t launch_check_roads(cudaStream_t s, const uint32_t* head, uint32_t n, uint32_t num_roads,
