@@ -17,6 +17,7 @@ constexpr uint32_t kRadix = 256;                            // 8-bit digits
 constexpr int kMaxPasses = 3;                               // keys up to 24 bits
 constexpr int kQueryThreads = 128;
 constexpr int kStepThreads = 512;  // measured at 16 M: 0.122 ms per tick against 0.136 with 256
+constexpr int kStepPer = 1;        // entities per thread and iteration of k_step
 constexpr int kMoveThreads = 128;  // move-only multi-tick launches (k_move)
 constexpr uint32_t kMaxCap = 256;
 constexpr uint32_t kPairBins = 256;  // pair counters (summed on read), spread to avoid one hot atomic
