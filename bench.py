@@ -201,6 +201,7 @@ def make_sim(pkg, cfg, road_map):
 
 def run_ours(args, cfg, world, rank, local):
     pkg = importlib.import_module("movement-sim_gb300")
+    pkg.set_device(local)  # the library's own CUDA runtime: select this rank's GPU there too
     road_map = pkg.RoadMap.lattice(cfg["lattice"], SEED)
     n = cfg["entities"]
     nbr = cfg["neighbours"]
@@ -369,6 +370,7 @@ def run_batched(args, world, rank, local):
     log-uniform 1e3..2e5, seed = index + SEED) advanced `steps` ticks by one
     persistent graph-captured launch, against one-at-a-time plain launches."""
     pkg = importlib.import_module("movement-sim_gb300")
+    pkg.set_device(local)
     sides, ents, seeds = ensemble_config(args.instances, SEED)
     maps = [pkg.RoadMap.lattice(s, sd) for s, sd in zip(sides, seeds)]
     total = sum(ents)
@@ -493,6 +495,7 @@ def run_adjoint(args, world, rank, local):
     import torch
 
     pkg = importlib.import_module("movement-sim_gb300")
+    pkg.set_device(local)
     cal = importlib.import_module("movement-sim_gb300.calibration")
     cfg = dict(CONFIGS["adjoint"])
     if args.ticks:
@@ -783,8 +786,8 @@ def main():
         return
     r = run_ours(args, cfg, world, rank, local)
     forms = None
-    if args.config == "scale" and not args.no_forms and not any(getattr(args, k) is not None
-                                                                 for k in ("entities", "lattice", "cap")):
+    if args.config == "scale" and world == 1 and not args.no_forms and not any(getattr(args, k) is not None
+                                                                               for k in ("entities", "lattice", "cap")):
         forms = run_forms(args, world, rank, local)
     if rank == 0:
         line.update({"value": r["value"], "ms_per_step": r["ms_per_step"], "roofline": r["roofline"],

@@ -141,6 +141,13 @@ typedef struct msim_init {
     float speed_max;    /* (1.4, 1.4) with dt = 1 reproduces SPEED, random_move.comp:750 */
 } msim_init;
 
+/* No counterpart in the reference (it drives one GPU through Kompute).  Selects the
+ * GPU that contexts, batches and calibrations created by the calling thread from now
+ * on use (the library carries its own CUDA runtime, so the application's
+ * cudaSetDevice does not reach it).  Device ids as cudaGetDeviceCount counts them;
+ * default 0. */
+int msim_set_device(int device);
+
 /* Replaces Simulator::init (src/sim/Simulator.cpp:44-106): copies the map to the
  * device (with one pad connection entry), allocates entity, index and neighbour
  * buffers.  Entities start zeroed; call msim_init_entities or msim_set_entities. */

@@ -21,7 +21,7 @@ from . import _capi
 from ._capi import (HEADING_ROAD_MASK, HEADING_TO_END, NO_NEIGHBOUR, PLACE_ROAD_START,  # noqa: F401
                     PLACE_UNIFORM_FRACTION, RNG_PCG32, RNG_XORSHIFT128, MsimError, check, lib)
 
-__all__ = ["RoadMap", "Simulation", "MsimError", "ENTITY_DTYPE", "RNG_XORSHIFT128", "RNG_PCG32",
+__all__ = ["RoadMap", "Simulation", "MsimError", "set_device", "ENTITY_DTYPE", "RNG_XORSHIFT128", "RNG_PCG32",
            "HEADING_TO_END", "HEADING_ROAD_MASK", "NO_NEIGHBOUR", "lib"]
 
 # Entity.hpp:33-46 (64-byte packed record)
@@ -61,6 +61,12 @@ def build_quad_tree(pos, width: float, height: float, max_depth: int = QUAD_TREE
 
 
 _RNG_KINDS = {"xorshift128": RNG_XORSHIFT128, "pcg32": RNG_PCG32}
+
+
+def set_device(device: int) -> None:
+    """The GPU that contexts created by this thread from now on use (msim_set_device);
+    the library's CUDA runtime does not follow torch.cuda.set_device."""
+    check(lib().msim_set_device(int(device)))
 
 
 def _ptr(a, ctype):

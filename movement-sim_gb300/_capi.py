@@ -76,6 +76,7 @@ SIGNATURES = {
     "msim_map_validate": (ctypes.c_int, [ctypes.POINTER(MsimMap)]),
     "msim_map_free": (None, [vp]),
     "msim_set_wait_limit": (ctypes.c_int, [vp, c_u32]),
+    "msim_set_device": (ctypes.c_int, [ctypes.c_int]),
     "msim_save_state": (ctypes.c_int, [vp, ctypes.c_char_p]),
     "msim_load_state": (ctypes.c_int, [vp, ctypes.c_char_p]),
     "msim_set_tick_timing": (ctypes.c_int, [vp, ctypes.c_int]),

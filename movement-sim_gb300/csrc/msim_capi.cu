@@ -1322,6 +1322,16 @@ int msim_get_tick_times(msim_ctx* c, float* update_ms, float* collision_ms) {
     return MSIM_OK;
 }
 
+int msim_set_device(int device) {
+    int count = 0;
+    cudaError_t e = cudaGetDeviceCount(&count);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaGetDeviceCount");
+    if (device < 0 || device >= count)
+        return fail(MSIM_ERR_INVALID, "device " + std::to_string(device) + " of " + std::to_string(count));
+    CK(cudaSetDevice(device), "cudaSetDevice");
+    return MSIM_OK;
+}
+
 int msim_set_wait_limit(msim_ctx* c, uint32_t polls) {
     int rc = check_ctx(c);
     if (rc != MSIM_OK) return rc;

@@ -144,3 +144,21 @@ def test_device_allocation_failure_everywhere(msim):
         sim.init_entities(SEED, placement="fraction", speed=SPEED)
         sim.step(3, neighbours=True)
         sim.sync()
+
+
+def test_set_device_checks_its_argument(msim):
+    """msim_set_device selects the library's GPU (its own CUDA runtime does not follow
+    the application's); ids outside the device count are rejected."""
+    torch = pytest.importorskip("torch")
+    count = torch.cuda.device_count()
+    msim.set_device(0)
+    for bad in (-1, count, count + 7):
+        with pytest.raises(msim.MsimError) as ei:
+            msim.set_device(bad)
+        assert ei.value.code == 1  # MSIM_ERR_INVALID
+    msim.set_device(0)
+    rm = msim.RoadMap.lattice(16, 3)
+    with msim.Simulation(rm, 2000, rng="pcg32", dt=0.1, radius=2.0, cap=8) as sim:
+        sim.init_entities(1, placement="fraction", speed=SPEED)
+        sim.step(2, neighbours=True)
+        sim.sync()
