@@ -211,7 +211,16 @@ int msim_get_neighbours(msim_ctx* ctx, uint32_t* count, uint32_t* idx);
  * on the host and uploads it first (Simulator.cpp:189-193).  The entities go in
  * chunks of at least 65,536 (up to 4): a chunk is moved as soon as it has arrived and
  * downloaded while later chunks still upload, so the two copy directions overlap;
- * the index and the query follow once every chunk has moved.  With page-locked host
+ * the index and the query follow once every chunk has moved.  When the previous call
+ * was also a neighbour host tick (and nothing moved or set the state since), the
+ * query reads the index built from the previous state, every box widened by this
+ * tick's largest displacement d (measured by the move, max(|dx|, |dy|) per entity;
+ * an entity within the radius of another lay within radius + d of it, in each
+ * coordinate, when that index was built), so the neighbour results are the same; the
+ * index of the new state is then built after the query, while the counts download
+ * and the next call's uploads run, and a device status it raises is reported by the
+ * next call.  A d above a quarter of the radius (large steps, host edits that move
+ * entities) takes the usual order for that tick.  With page-locked host
  * buffers (msim_host_alloc) the copies run asynchronously; pageable ones work too.
  * in_speed may be NULL (1.4 m per tick at dt = 1); any output may be NULL; out_count
  * and out_idx need MSIM_STEP_NEIGHBOURS.  in_pos / out_pos (and heading, rng) may be
@@ -315,6 +324,11 @@ const char* msim_kernel_name(uint32_t kernel);
  * whose key changed per incremental update): the sort's work per tick.
  * Synchronises the context's stream. */
 int msim_get_sort_stats(msim_ctx* ctx, uint64_t* index_updates, uint64_t* sorted_entries);
+/* msim_tick_host calls since the stats were reset, those whose query read the
+ * previous state's index with widened boxes, and the largest displacement measured by
+ * the last call that measured one (any pointer may be NULL; reset with the kernel
+ * stats). */
+int msim_get_host_tick_stats(msim_ctx* ctx, uint64_t* host_ticks, uint64_t* skin_queries, float* last_displacement);
 
 /* Events on the context's stream around a region of queued work (bench timing). */
 int msim_timer_begin(msim_ctx* ctx);

@@ -338,6 +338,13 @@ class Simulation:
         check(lib().msim_get_sort_stats(self._ctx, ctypes.byref(u), ctypes.byref(e)))
         return {"index_updates": u.value, "sorted_entries": e.value}
 
+    def host_tick_stats(self) -> dict:
+        """Host ticks since the stats were reset, those whose query read the previous
+        state's index with widened boxes, and the last measured displacement."""
+        h, s, d = ctypes.c_uint64(), ctypes.c_uint64(), ctypes.c_float()
+        check(lib().msim_get_host_tick_stats(self._ctx, ctypes.byref(h), ctypes.byref(s), ctypes.byref(d)))
+        return {"host_ticks": h.value, "skin_queries": s.value, "last_displacement": d.value}
+
     def timer_begin(self) -> None:
         check(lib().msim_timer_begin(self._ctx))
 

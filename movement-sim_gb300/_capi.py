@@ -102,6 +102,8 @@ SIGNATURES = {
     "msim_reset_kernel_stats": (ctypes.c_int, [vp]),
     "msim_get_kernel_stats": (ctypes.c_int, [vp, c_u32, ctypes.POINTER(c_u64), ctypes.POINTER(ctypes.c_double)]),
     "msim_get_sort_stats": (ctypes.c_int, [vp, ctypes.POINTER(c_u64), ctypes.POINTER(c_u64)]),
+    "msim_get_host_tick_stats": (ctypes.c_int, [vp, ctypes.POINTER(c_u64), ctypes.POINTER(c_u64),
+                                                ctypes.POINTER(ctypes.c_float)]),
     "msim_tick_host": (ctypes.c_int, [vp, f32p, u32p, u32p, f32p, c_u32, f32p, u32p, u32p, u32p, u32p]),
     "msim_kernel_count": (c_u32, []),
     "msim_kernel_name": (ctypes.c_char_p, [c_u32]),

@@ -55,11 +55,12 @@ enum KernelId : uint32_t {
     K_EXPORT,
     K_MARK,   // split of the previous order into unchanged / changed keys
     K_MERGE,  // merge + key-start table + sorted positions
+    K_GATHER, // host tick: an uploaded chunk's positions into the previous sorted order
     K_COUNT
 };
 static const char* const kKernelNames[K_COUNT] = {"k_init",   "k_step",   "k_step_multi", "k_onesweep",
                                                   "k_kstart", "k_query",  "k_permute",    "k_export",
-                                                  "k_mark",   "k_merge"};
+                                                  "k_mark",   "k_merge",  "k_gather"};
 
 // msim_tick_host: at most this many chunks, each at least kHostChunkMin entities
 constexpr uint32_t kHostChunks = 4;  // at 16 M: 4.09 ms per host tick; 8 chunks 4.16-4.18, 16 4.31
@@ -131,7 +132,23 @@ struct msim_ctx {
     unsigned long long* sorted_dev = nullptr;
     uint64_t sorted_host = 0;
     uint64_t index_updates = 0;
+    // Host ticks that query the previous index (the skin query): index_on_state = the
+    // current index was built from the keys of the current state (slot = id, nothing
+    // moved or set since); skin_pos = the new positions in that index's sorted order;
+    // disp = the tick's largest displacement (device word, float bits); disp_host =
+    // page-locked words: [0] its copy, [1] the device status as the query left it.
+    bool index_on_state = false;
+    bool state_free_event = false;
+    uint64_t host_ticks = 0, skin_queries = 0;  // since the stats were reset
+    float last_disp = 0.f;  // ev_state_free marks the last read of the spare state buffer
+    float2* skin_pos = nullptr;
+    uint32_t* disp = nullptr;
+    uint32_t* disp_host = nullptr;
+    cudaEvent_t ev_disp = nullptr, ev_query = nullptr, ev_state_free = nullptr;
     // neighbours
+    // query_slot: the sorted slots of the index the last query ran on (its counts and
+    // lists are in that order; a host tick's background update moves sorted_slot on)
+    const uint32_t* query_slot = nullptr;
     uint32_t* nbr_count = nullptr;
     uint32_t* nbr_list = nullptr;
     unsigned long long* pairs = nullptr;
@@ -243,6 +260,10 @@ void free_all(msim_ctx* c) {
         if (c->ev_up[k]) cudaEventDestroy(c->ev_up[k]);
         if (c->ev_moved[k]) cudaEventDestroy(c->ev_moved[k]);
     }
+    for (cudaEvent_t e : {c->ev_disp, c->ev_query, c->ev_state_free})
+        if (e) cudaEventDestroy(e);
+    if (c->disp_host) cudaFreeHost(c->disp_host);
+    c->disp_host = nullptr;
     if (c->up) cudaStreamDestroy(c->up);
     if (c->down) cudaStreamDestroy(c->down);
     if (c->stream) cudaStreamDestroy(c->stream);
@@ -318,6 +339,40 @@ int ensure_stage(msim_ctx* c, size_t bytes) {
 }
 
 EntityState& cur_state(msim_ctx* c) { return c->st[c->cur]; }
+
+// Skin query of a host tick: allowed while the tick's largest displacement is at most
+// this fraction of the reach (the boxes grow by it; at the 16 M workload d is about
+// 0.16 m against a reach of 2 m).
+constexpr float kSkinFraction = 0.25f;
+
+// Buffers of the skin query (allocated by the first host tick that can use it): false
+// when an allocation fails, and the tick then takes the usual order.
+bool ensure_skin(msim_ctx* c) {
+    if (c->skin_pos && c->disp && c->disp_host) return true;
+    if (!c->skin_pos) {
+        void* raw = nullptr;
+        if (!device_malloc(&raw, sizeof(float2) * std::max<size_t>(c->n, 1))) return false;
+        c->allocs.push_back(raw);
+        c->device_bytes += sizeof(float2) * std::max<size_t>(c->n, 1);
+        c->skin_pos = static_cast<float2*>(raw);
+    }
+    if (!c->disp) {
+        void* raw = nullptr;
+        if (!device_malloc(&raw, sizeof(uint32_t))) return false;
+        c->allocs.push_back(raw);
+        c->device_bytes += sizeof(uint32_t);
+        c->disp = static_cast<uint32_t*>(raw);
+    }
+    if (!c->disp_host) {
+        void* h = nullptr;
+        if (cudaMallocHost(&h, 2 * sizeof(uint32_t)) != cudaSuccess) {
+            cudaGetLastError();
+            return false;
+        }
+        c->disp_host = static_cast<uint32_t*>(h);
+    }
+    return true;
+}
 
 StepLaunch step_args(msim_ctx* c, uint32_t ticks, bool key) {
     StepLaunch a;
@@ -463,6 +518,8 @@ int permute_state(msim_ctx* c) {
 // Forget the index (new entity state in slot = id order): the next neighbour tick
 // runs a full sort, and the one after re-orders the state by it.
 void reset_index(msim_ctx* c) {
+    c->index_on_state = false;
+    c->state_free_event = false;
     c->have_nbr = false;
     c->have_sort = false;
     c->sorted_key = nullptr;
@@ -475,6 +532,8 @@ void reset_index(msim_ctx* c) {
 // tree (random_move.comp:863-867); here: sort by tile and re-order the state.
 int build_index(msim_ctx* c) {
     c->have_nbr = false;
+    c->index_on_state = false;
+    c->state_free_event = false;
     if (c->n == 0) return MSIM_OK;
     int rc = sort_entities(c, 0);
     if (rc != MSIM_OK) return rc;
@@ -486,7 +545,7 @@ int build_index(msim_ctx* c) {
 // table and the sorted positions on the way).  The update's scratch (digit counts,
 // split ticket and look-back words) is cleared first, in one memset, before the
 // move, so that the move step and the split run back to back.
-int incremental_update(msim_ctx* c);
+int incremental_update(msim_ctx* c, bool positions = true);
 
 int clear_update_scratch(msim_ctx* c) {
     CK(cudaMemsetAsync(c->hist, 0, sizeof(uint32_t) * c->update_words, c->stream), "memset update scratch");
@@ -511,8 +570,10 @@ int incremental_index(msim_ctx* c) {
     return incremental_update(c);
 }
 
-// The update itself, for new keys (by slot) already in c->key.
-int incremental_update(msim_ctx* c) {
+// The update itself, for new keys (by slot) already in c->key.  positions = false:
+// the sorted positions are not written (a host tick whose next query reads the
+// positions it gathers itself).
+int incremental_update(msim_ctx* c, bool positions) {
     NvtxRange range("msim index update");
     int rc = inject_sort_tile(c, c->mark_ticket);
     if (rc != MSIM_OK) return rc;
@@ -547,7 +608,8 @@ int incremental_update(msim_ctx* c) {
         Prof p(c, K_MERGE);
         uint32_t launched = 0;
         CKL(p, launch_merge(c->stream, c->a_key, c->a_val, c->b_key[c->passes & 1], c->b_val[c->passes & 1],
-                        c->ab_counts, c->merge_split, c->n, c->sk[out], c->sv[out], cur_state(c).pos, c->sorted_pos,
+                        c->ab_counts, c->merge_split, c->n, c->sk[out], c->sv[out],
+                        positions ? cur_state(c).pos : nullptr, positions ? c->sorted_pos : nullptr,
                         c->kstart, (uint32_t)c->num_keys, c->kstart_chunks, c->kstart_chunk_count, c->err,
                         &launched, c->chunk_count_zeroed),
            "k_merge");
@@ -562,7 +624,8 @@ int incremental_update(msim_ctx* c) {
 }
 
 int key_start_table(msim_ctx* c);
-int run_query(msim_ctx* c, bool overlap, uint32_t* count_by_id = nullptr);
+int run_query(msim_ctx* c, bool overlap, uint32_t* count_by_id = nullptr, const float2* pos = nullptr,
+              const TileGrid* grid = nullptr);
 
 int neighbour_tick(msim_ctx* c) {
     NvtxRange range("msim neighbour tick");
@@ -600,7 +663,9 @@ int key_start_table(msim_ctx* c) {
 
 // The radius query over the index just built.
 // count_by_id (only with slots holding their own entity): the counts also by id.
-int run_query(msim_ctx* c, bool overlap, uint32_t* count_by_id) {
+// pos / grid (may be NULL): the positions in sorted order and the grid (its reach)
+// instead of the index's own (the skin query of a host tick).
+int run_query(msim_ctx* c, bool overlap, uint32_t* count_by_id, const float2* pos, const TileGrid* grid) {
     NvtxRange range("msim query");
     // The query reads only the index (key-start table, sorted slots and positions)
     // and slot ids: the next tick's move step may overwrite positions meanwhile.  With
@@ -615,8 +680,8 @@ int run_query(msim_ctx* c, bool overlap, uint32_t* count_by_id) {
     {
         Prof p(c, K_QUERY);
         // slots that hold their own entity need no id lookup
-        CKL(p, launch_query(qs, c->params.cap, c->kstart, c->sorted_slot, c->sorted_pos,
-                        c->slots_identity ? nullptr : cur_state(c).slot_id, c->grid,
+        CKL(p, launch_query(qs, c->params.cap, c->kstart, c->sorted_slot, pos ? pos : c->sorted_pos,
+                        c->slots_identity ? nullptr : cur_state(c).slot_id, grid ? *grid : c->grid,
                         c->n, c->nbr_count, c->nbr_list, c->pairs, c->err,
                         c->slots_identity ? count_by_id : nullptr),
            "k_query");
@@ -629,6 +694,7 @@ int run_query(msim_ctx* c, bool overlap, uint32_t* count_by_id) {
         CK(cudaEventRecord(c->ev_tick[2], qs), "cudaEventRecord");
         c->tick_recorded = true;
     }
+    c->query_slot = c->sorted_slot;
     c->have_nbr = true;
     c->since_permute++;
     return MSIM_OK;
@@ -927,6 +993,8 @@ int msim_step(msim_ctx* c, uint32_t ticks, uint32_t flags) {
         c->tick += ticks;
         return MSIM_OK;
     }
+    c->index_on_state = false;  // (a neighbour tick may also re-order the state)
+    c->state_free_event = false;
     if (flags & MSIM_STEP_NEIGHBOURS) {
         for (uint32_t t = 0; t < ticks; t++) {
             rc = neighbour_tick(c);
@@ -999,7 +1067,7 @@ int msim_get_neighbours(msim_ctx* c, uint32_t* count, uint32_t* idx) {
     uint32_t* d_idx = want_idx ? d_count + n : nullptr;
     {
         Prof p(c, K_EXPORT);
-        CK(launch_export_neighbours(c->stream, c->sorted_slot, cur_state(c).slot_id, c->nbr_count, c->nbr_list,
+        CK(launch_export_neighbours(c->stream, c->query_slot, cur_state(c).slot_id, c->nbr_count, c->nbr_list,
                                     c->n, c->params.cap, d_count, d_idx),
            "k_export_nbr");
     }
@@ -1029,6 +1097,9 @@ int msim_tick_host(msim_ctx* c, const float* in_pos, const uint32_t* in_heading,
         CK(cudaStreamCreateWithFlags(&c->up, cudaStreamNonBlocking), "cudaStreamCreate");
         CK(cudaStreamCreateWithFlags(&c->down, cudaStreamNonBlocking), "cudaStreamCreate");
         CK(cudaEventCreateWithFlags(&c->ev_start, cudaEventDisableTiming), "cudaEventCreate");
+        CK(cudaEventCreateWithFlags(&c->ev_disp, cudaEventDisableTiming), "cudaEventCreate");
+        CK(cudaEventCreateWithFlags(&c->ev_query, cudaEventDisableTiming), "cudaEventCreate");
+        CK(cudaEventCreateWithFlags(&c->ev_state_free, cudaEventDisableTiming), "cudaEventCreate");
         for (uint32_t k = 0; k < kHostChunks; k++) {
             CK(cudaEventCreateWithFlags(&c->ev_up[k], cudaEventDisableTiming), "cudaEventCreate");
             CK(cudaEventCreateWithFlags(&c->ev_moved[k], cudaEventDisableTiming), "cudaEventCreate");
@@ -1045,6 +1116,20 @@ int msim_tick_host(msim_ctx* c, const float* in_pos, const uint32_t* in_heading,
     // followed by one tick): the new state goes to the same slots.
     const bool old_slots_identity = c->slots_identity;
     const bool use_inc = nbr && c->incremental && c->sorted_key && c->slots_identity;
+    // Skin query: when the current index was built from the keys of the state this
+    // tick starts from (the previous call was a neighbour host tick and nothing moved
+    // or set the state since), this tick's query reads that index with every box
+    // widened by the tick's largest displacement d (an entity within the radius of
+    // another now lay within radius + d of it when the index was built, in each
+    // coordinate).  The move measures d; the new positions are gathered into the
+    // index's order chunk by chunk behind the uploads; the index update for the new
+    // state then runs after the query, beside the downloads and the next call's
+    // uploads.  A d above a quarter of the reach (host edits between ticks, large
+    // steps) takes the usual order: index update, then query.
+    const bool state_free_event = c->state_free_event;
+    bool skin = use_inc && c->index_on_state && c->grid.reach > 0.f && ensure_skin(c);
+    c->index_on_state = false;
+    c->state_free_event = false;
     // In place (the same page-locked arrays for heading and RNG in and out): they
     // already hold every value the tick leaves unchanged, so the move kernel writes the
     // headings and RNG states that change (entities at a road end, a few per thousand
@@ -1065,16 +1150,24 @@ int msim_tick_host(msim_ctx* c, const float* in_pos, const uint32_t* in_heading,
     CK(cudaMemsetAsync(c->check, 0xff, sizeof(uint32_t), c->stream), "memset check");
     if (nbr && !use_inc) CK(cudaMemsetAsync(c->hist, 0, sizeof(uint32_t) * kMaxPasses * kRadix, c->stream), "memset hist");
     if (use_inc && (rc = clear_update_scratch(c)) != MSIM_OK) return rc;
+    if (skin) CK(cudaMemsetAsync(c->disp, 0, sizeof(uint32_t), c->stream), "memset displacement");
     // entity i in slot i (for later calls; this tick's query and export take the slot
     // as the id): written first, beside the first chunk's upload
     CK(launch_iota(c->stream, s.slot_id, n), "k_iota");
-    CK(cudaEventRecord(c->ev_start, c->stream), "cudaEventRecord");
-    CK(cudaStreamWaitEvent(c->up, c->ev_start, 0), "cudaStreamWaitEvent");
+    if (state_free_event) {
+        // the last read of the spare buffer was recorded before the previous call's
+        // index update, which so runs beside these uploads
+        CK(cudaStreamWaitEvent(c->up, c->ev_state_free, 0), "cudaStreamWaitEvent");
+    } else {
+        CK(cudaEventRecord(c->ev_start, c->stream), "cudaEventRecord");
+        CK(cudaStreamWaitEvent(c->up, c->ev_start, 0), "cudaStreamWaitEvent");
+    }
 
     // chunk k: upload (up) -> check headings, move, key, digit counts (stream) ->
     // download of the moved state (down); chunk k's download overlaps chunk k+1's upload
     const uint32_t chunk = std::max<uint32_t>(kHostChunkMin, (n + kHostChunks - 1) / kHostChunks);
     uint32_t k = 0;
+    uint32_t last_lo = 0, last_cnt = 0;
     for (uint32_t lo = 0; lo < n; lo += chunk, k++) {
         const uint32_t cnt = std::min(chunk, n - lo);
         CK(cudaMemcpyAsync(s.head + lo, in_heading + lo, sizeof(uint32_t) * cnt, cudaMemcpyHostToDevice, c->up),
@@ -1105,6 +1198,10 @@ int msim_tick_host(msim_ctx* c, const float* in_pos, const uint32_t* in_heading,
             a.host_head = dev_head;
             a.host_rng = dev_rng;
             a.id_base = lo;
+            if (skin) {  // displacement against the positions the current index was built from
+                a.index_pos = c->st[old].pos + lo;
+                a.disp_max = c->disp;
+            }
             CK(launch_step(c->stream, a), "k_step");
         }
         CK(cudaEventRecord(c->ev_moved[k], c->stream), "cudaEventRecord");
@@ -1113,57 +1210,112 @@ int msim_tick_host(msim_ctx* c, const float* in_pos, const uint32_t* in_heading,
             CK(cudaMemcpyAsync(out_pos + 2 * (size_t)lo, s.pos + lo, sizeof(float2) * cnt, cudaMemcpyDeviceToHost,
                                c->down),
                "download pos");
-        if (in_place) continue;  // headings and RNG states: written by the move kernel
-        if (out_heading)
-            CK(cudaMemcpyAsync(out_heading + lo, s.head + lo, sizeof(uint32_t) * cnt, cudaMemcpyDeviceToHost, c->down),
-               "download heading");
-        if (out_rng)
-            CK(cudaMemcpyAsync(out_rng + 4 * (size_t)lo, s.rng + lo, sizeof(uint4) * cnt, cudaMemcpyDeviceToHost,
-                               c->down),
-               "download rng");
+        if (!in_place) {  // headings and RNG states in place: written by the move kernel
+            if (out_heading)
+                CK(cudaMemcpyAsync(out_heading + lo, s.head + lo, sizeof(uint32_t) * cnt, cudaMemcpyDeviceToHost,
+                                   c->down),
+                   "download heading");
+            if (out_rng)
+                CK(cudaMemcpyAsync(out_rng + 4 * (size_t)lo, s.rng + lo, sizeof(uint4) * cnt,
+                                   cudaMemcpyDeviceToHost, c->down),
+                   "download rng");
+        }
+        last_lo = lo;
+        last_cnt = cnt;
+        if (skin && lo + cnt < n) {  // the last chunk's gather runs while the host reads d
+            Prof p(c, K_GATHER);
+            CK(launch_gather_chunk(c->stream, c->sorted_slot, n, lo, cnt, s.pos, c->skin_pos), "k_gather_chunk");
+        }
     }
     c->cur = b;
     c->slots_identity = true;
-    if (use_inc) {
-        if ((rc = incremental_update(c)) != MSIM_OK) return rc;
-    } else {
-        reset_index(c);
-        if (nbr && ((rc = sort_keys(c)) != MSIM_OK || (rc = key_start_table(c)) != MSIM_OK)) return rc;
+    TileGrid skin_grid = c->grid;
+    if (skin) {
+        CK(cudaMemcpyAsync(c->disp_host, c->disp, sizeof(uint32_t), cudaMemcpyDeviceToHost, c->stream),
+           "read displacement");
+        CK(cudaEventRecord(c->ev_disp, c->stream), "cudaEventRecord");
+        {
+            Prof p(c, K_GATHER);
+            CK(launch_gather_chunk(c->stream, c->sorted_slot, n, last_lo, last_cnt, s.pos, c->skin_pos),
+               "k_gather_chunk");
+        }
+        CK(cudaEventSynchronize(c->ev_disp), "cudaEventSynchronize");
+        float d = 0.f;
+        std::memcpy(&d, c->disp_host, sizeof(d));
+        c->last_disp = d;
+        skin = d <= kSkinFraction * c->grid.reach;  // false for +inf (a non-finite position)
+        if (skin) {
+            // widened reach, rounded up: the displacement was measured with one rounding
+            const double r = (double)c->grid.reach + (double)d * (1.0 + 0x1p-20);
+            float rf = (float)r;
+            if ((double)rf < r) rf = std::nextafter(rf, INFINITY);
+            skin_grid.reach = rf;
+        }
     }
-    if (nbr) {
-        const bool want_idx = out_idx && c->params.cap;
-        const size_t cap = c->params.cap;
-        uint32_t* d_count = nullptr;
-        if (out_count || out_idx) {
-            if ((rc = ensure_stage(c, (size_t)n * sizeof(uint32_t) * (1 + (want_idx ? cap : 0)))) != MSIM_OK)
-                return rc;
-            d_count = static_cast<uint32_t*>(c->stage);
+    const bool want_idx = nbr && out_idx && c->params.cap;
+    const size_t cap = c->params.cap;
+    uint32_t* d_count = nullptr;
+    if (nbr && (out_count || out_idx)) {
+        if ((rc = ensure_stage(c, (size_t)n * sizeof(uint32_t) * (1 + (want_idx ? cap : 0)))) != MSIM_OK) return rc;
+        d_count = static_cast<uint32_t*>(c->stage);
+    }
+    uint32_t* d_idx = want_idx ? d_count + n : nullptr;
+    // the neighbour downloads go on `dl`: the context's stream, or (skin query) the
+    // download stream, so the index update can follow the query on the context's stream
+    cudaStream_t dl = c->stream;
+    if (nbr && skin) {
+        // slots hold entity ids: the query writes the counts by id itself
+        if ((rc = run_query(c, false, d_count, c->skin_pos, &skin_grid)) != MSIM_OK) return rc;
+        if (want_idx) {
+            Prof p(c, K_EXPORT);
+            CK(launch_export_neighbours(c->stream, c->query_slot, nullptr, c->nbr_count, c->nbr_list, n,
+                                        c->params.cap, d_count, d_idx),
+               "k_export_nbr");
+        }
+        // the status as the query left it, before the index update below can raise one
+        CK(cudaMemcpyAsync(c->disp_host + 1, c->err, sizeof(uint32_t), cudaMemcpyDeviceToHost, c->stream),
+           "read device status");
+        CK(cudaEventRecord(c->ev_query, c->stream), "cudaEventRecord");
+        CK(cudaStreamWaitEvent(c->down, c->ev_query, 0), "cudaStreamWaitEvent");
+        // nothing after this point reads the spare state buffer: the next call's uploads
+        // may start while the index update below runs
+        CK(cudaEventRecord(c->ev_state_free, c->stream), "cudaEventRecord");
+        dl = c->down;
+    } else if (nbr) {
+        if (use_inc) {
+            if ((rc = incremental_update(c)) != MSIM_OK) return rc;
+        } else {
+            reset_index(c);
+            if ((rc = sort_keys(c)) != MSIM_OK || (rc = key_start_table(c)) != MSIM_OK) return rc;
         }
         // slots hold entity ids here: the query writes the counts by id itself, so with
         // counts alone no export pass runs between the query and their download
         if ((rc = run_query(c, false, d_count)) != MSIM_OK) return rc;
-        if (out_count || out_idx) {
-            uint32_t* d_idx = want_idx ? d_count + n : nullptr;
-            if (want_idx) {
-                Prof p(c, K_EXPORT);
-                CK(launch_export_neighbours(c->stream, c->sorted_slot, nullptr, c->nbr_count, c->nbr_list, n,
-                                            c->params.cap, d_count, d_idx),
-                   "k_export_nbr");
-            }
-            if (out_count)
-                CK(cudaMemcpyAsync(out_count, d_count, sizeof(uint32_t) * n, cudaMemcpyDeviceToHost, c->stream),
-                   "download counts");
-            if (want_idx)
-                CK(cudaMemcpyAsync(out_idx, d_idx, sizeof(uint32_t) * n * cap, cudaMemcpyDeviceToHost, c->stream),
-                   "download neighbours");
+        if (want_idx) {
+            Prof p(c, K_EXPORT);
+            CK(launch_export_neighbours(c->stream, c->query_slot, nullptr, c->nbr_count, c->nbr_list, n,
+                                        c->params.cap, d_count, d_idx),
+               "k_export_nbr");
         }
+    } else {
+        reset_index(c);
     }
+    if (out_count) CK(cudaMemcpyAsync(out_count, d_count, sizeof(uint32_t) * n, cudaMemcpyDeviceToHost, dl), "download counts");
+    if (want_idx)
+        CK(cudaMemcpyAsync(out_idx, d_idx, sizeof(uint32_t) * n * cap, cudaMemcpyDeviceToHost, dl),
+           "download neighbours");
+    // the index of the new state for the next call (no sorted positions: its query
+    // gathers its own); with the skin query this runs after the query, off the host's path
+    if (nbr && skin && (rc = incremental_update(c, false)) != MSIM_OK) return rc;
     c->tick++;
     uint32_t first_bad = 0;
-    CK(cudaMemcpyAsync(&first_bad, c->check, sizeof(first_bad), cudaMemcpyDeviceToHost, c->stream), "read check");
+    // read after the query: the heading checks of every chunk ran before it
+    CK(cudaMemcpyAsync(&first_bad, c->check, sizeof(first_bad), cudaMemcpyDeviceToHost, dl), "read check");
     CK(cudaStreamSynchronize(c->down), "cudaStreamSynchronize");
-    CK(cudaStreamSynchronize(c->stream), "cudaStreamSynchronize");
+    if (!skin) CK(cudaStreamSynchronize(c->stream), "cudaStreamSynchronize");
+    const uint32_t status = skin ? c->disp_host[1] : 0u;
     if (first_bad != 0xffffffffu) {  // as msim_set_entities: the previous state stays
+        CK(cudaStreamSynchronize(c->stream), "cudaStreamSynchronize");
         c->cur = old;
         reset_index(c);
         c->slots_identity = old_slots_identity;
@@ -1174,7 +1326,22 @@ int msim_tick_host(msim_ctx* c, const float* in_pos, const uint32_t* in_heading,
                                       std::to_string(in_heading[first_bad] & MSIM_HEADING_ROAD_MASK) + " of " +
                                       std::to_string(c->R));
     }
-    return sync_and_check(c);
+    if (skin) {
+        // a status raised before the query (e.g. by the previous call's index update):
+        // reported now, after everything on the context's stream
+        if (status) return sync_and_check(c);
+        c->index_on_state = true;
+        c->state_free_event = true;
+        c->host_ticks++;
+        c->skin_queries++;
+        return MSIM_OK;
+    }
+    rc = sync_and_check(c);
+    if (rc == MSIM_OK) {
+        c->index_on_state = nbr;  // the index was built from this state
+        c->host_ticks++;
+    }
+    return rc;
 }
 
 int msim_get_collision_pairs(msim_ctx* c, uint64_t* pairs) {
@@ -1201,7 +1368,7 @@ int msim_export_entities_aos(msim_ctx* c, void* out, size_t n) {
     {
         Prof p(c, K_EXPORT);
         CK(launch_export_aos(c->stream, c->dmap(), cur_state(c), c->n, c->params.dt,
-                             c->have_nbr ? c->sorted_slot : nullptr, c->have_nbr ? c->nbr_count : nullptr, c->stage),
+                             c->have_nbr ? c->query_slot : nullptr, c->have_nbr ? c->nbr_count : nullptr, c->stage),
            "k_export_aos");
     }
     CK(cudaMemcpyAsync(out, c->stage, n * 64, cudaMemcpyDeviceToHost, c->stream), "download entities");
@@ -1370,8 +1537,18 @@ int msim_reset_kernel_stats(msim_ctx* c) {
     }
     c->sorted_host = 0;
     c->index_updates = 0;
+    c->host_ticks = 0;
+    c->skin_queries = 0;
     CK(cudaMemsetAsync(c->sorted_dev, 0, sizeof(unsigned long long), c->stream), "memset sort stats");
     return rc;
+}
+
+int msim_get_host_tick_stats(msim_ctx* c, uint64_t* host_ticks, uint64_t* skin_queries, float* last_displacement) {
+    if (!c) return fail(MSIM_ERR_INVALID, "context is NULL");
+    if (host_ticks) *host_ticks = c->host_ticks;
+    if (skin_queries) *skin_queries = c->skin_queries;
+    if (last_displacement) *last_displacement = c->last_disp;
+    return MSIM_OK;
 }
 
 int msim_get_sort_stats(msim_ctx* c, uint64_t* index_updates, uint64_t* sorted_entries) {

@@ -334,21 +334,32 @@ __global__ __launch_bounds__(kMergeThreads, 8) void k_merge(
     __syncthreads();
     const uint32_t cnt = d1 - d0;
     const uint32_t prev_tile = s_prev;
-    float2 gp[kPer];  // the positions of a thread's outputs, gathered together
+    if (sorted_pos) {
+        float2 gp[kPer];  // the positions of a thread's outputs, gathered together
 #pragma unroll
-    for (uint32_t k = 0; k < kPer; k++) {
-        const uint32_t i = k * kMergeThreads + tid;
-        const uint32_t slot = i < cnt ? s_outv[i] : n;
-        gp[k] = slot < n ? pos[slot] : make_float2(__int_as_float(0x7fffffff), __int_as_float(0x7fffffff));
-    }
+        for (uint32_t k = 0; k < kPer; k++) {
+            const uint32_t i = k * kMergeThreads + tid;
+            const uint32_t slot = i < cnt ? s_outv[i] : n;
+            gp[k] = slot < n ? pos[slot] : make_float2(__int_as_float(0x7fffffff), __int_as_float(0x7fffffff));
+        }
 #pragma unroll
-    for (uint32_t k = 0; k < kPer; k++) {  // sorted keys, slots and positions: coalesced rows
-        const uint32_t i = k * kMergeThreads + tid;
-        if (i < cnt) {
-            const uint32_t p = d0 + i;
-            out_key[p] = s_outk[i];
-            out_val[p] = s_outv[i];
-            sorted_pos[p] = gp[k];
+        for (uint32_t k = 0; k < kPer; k++) {  // sorted keys, slots and positions: coalesced rows
+            const uint32_t i = k * kMergeThreads + tid;
+            if (i < cnt) {
+                const uint32_t p = d0 + i;
+                out_key[p] = s_outk[i];
+                out_val[p] = s_outv[i];
+                sorted_pos[p] = gp[k];
+            }
+        }
+    } else {  // an index whose query reads the positions from elsewhere
+#pragma unroll
+        for (uint32_t k = 0; k < kPer; k++) {
+            const uint32_t i = k * kMergeThreads + tid;
+            if (i < cnt) {
+                out_key[d0 + i] = s_outk[i];
+                out_val[d0 + i] = s_outv[i];
+            }
         }
     }
     // Key-start entries: position p owns the entries (key[p-1], key[p]], so the kPer

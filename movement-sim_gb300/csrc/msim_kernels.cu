@@ -190,16 +190,20 @@ __global__ __launch_bounds__(kMoveThreads) void k_move(StepLaunch a) {
 // kStepPer entities per thread and iteration (slots s, s + stride, ...), their loads
 // in flight before any is stepped.  One per thread at four 512-thread blocks per SM
 // (32 registers): 0.122 ms at 16 M against 0.125 for two per thread at three blocks.
-template <int RNG, bool KEY>
+// DISP: the tick's largest displacement is measured too (StepLaunch::disp_max).
+template <int RNG, bool KEY, bool DISP>
 __global__ __launch_bounds__(kStepThreads, 4) void k_step(StepLaunch a) {
     __shared__ uint32_t s_hist[kMaxPasses * kRadix];
     __shared__ uint32_t s_morton[KEY ? 2048 : 1];
+    __shared__ uint32_t s_disp;
     if (KEY) {  // shared memory only: overlaps the predecessor's tail
         for (uint32_t i = threadIdx.x; i < a.passes * kRadix; i += kStepThreads) s_hist[i] = 0u;
         for (uint32_t i = threadIdx.x; i < 2048u; i += kStepThreads) s_morton[i] = part1by1(i);
+        if (DISP && threadIdx.x == 0) s_disp = 0u;
         __syncthreads();
     }
     chain_enter();
+    uint32_t dbits = 0u;  // DISP: this thread's largest displacement (non-negative float bits order as floats)
     const uint32_t lane = threadIdx.x & 31;
     const uint32_t stride = gridDim.x * kStepThreads;
     for (uint32_t i = blockIdx.x * kStepThreads + threadIdx.x; i < a.zero_a_words; i += stride) a.zero_a[i] = 0u;
@@ -254,6 +258,22 @@ __global__ __launch_bounds__(kStepThreads, 4) void k_step(StepLaunch a) {
 #pragma unroll
             for (int u = 0; u < kStepPer; u++) digit_counts<RNG, KEY>(key[u], valid[u], lane, a.passes, s_hist);
         }
+        if (DISP) {
+#pragma unroll
+            for (int u = 0; u < kStepPer; u++) {
+                if (!valid[u]) continue;
+                const float2 o = a.index_pos[sl[u]];
+                const float dx = fabsf(__fsub_rn(p[u].x, o.x)), dy = fabsf(__fsub_rn(p[u].y, o.y));
+                const uint32_t b = dx <= 3.0e38f && dy <= 3.0e38f ? __float_as_uint(fmaxf(dx, dy)) : 0x7f800000u;
+                dbits = b > dbits ? b : dbits;
+            }
+        }
+    }
+    if (DISP) {  // one global atomic per block (one per warp serialised on the word: 0.08 ms per 4 M)
+        dbits = __reduce_max_sync(0xffffffffu, dbits);
+        if (lane == 0 && dbits) atomicMax(&s_disp, dbits);
+        __syncthreads();
+        if (threadIdx.x == 0 && s_disp) atomicMax(a.disp_max, s_disp);
     }
     if (KEY && a.hist) {
         __syncthreads();
@@ -666,6 +686,27 @@ __global__ void k_fill_f32(float* out, uint32_t n, float v) {
     if (i < n) out[i] = v;
 }
 
+// out[q] = pos[P[q]] where lo <= P[q] < lo + cnt (host tick, one uploaded chunk):
+// kGatherPer rows of 256 consecutive q per thread and round, every slot load of a
+// thread issued before its position loads.
+constexpr uint32_t kGatherPer = 4;
+__global__ __launch_bounds__(256) void k_gather_chunk(const uint32_t* __restrict__ P, uint32_t n, uint32_t lo,
+                                                      uint32_t cnt, const float2* __restrict__ pos,
+                                                      float2* __restrict__ out) {
+    const uint32_t stride = gridDim.x * 256u * kGatherPer;
+    for (uint32_t base = blockIdx.x * 256u * kGatherPer + threadIdx.x; base < n; base += stride) {
+        uint32_t sl[kGatherPer];
+#pragma unroll
+        for (uint32_t k = 0; k < kGatherPer; k++) {
+            const uint32_t q = base + k * 256u;
+            sl[k] = q < n ? P[q] - lo : 0xffffffffu;  // chunk-relative slot (wraps below lo)
+        }
+#pragma unroll
+        for (uint32_t k = 0; k < kGatherPer; k++)
+            if (sl[k] < cnt) out[base + k * 256u] = pos[lo + sl[k]];
+    }
+}
+
 __global__ void k_iota(uint32_t* out, uint32_t n) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) out[i] = i;
@@ -697,7 +738,7 @@ cudaError_t configure_kernels(uint32_t) { return cudaSuccess; }
 int step_blocks_for(int device, uint32_t n) {
     int sms = 0, per_sm = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_step<0, true>, kStepThreads, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_step<0, true, false>, kStepThreads, 0);
     if (sms <= 0) sms = 1;
     if (per_sm <= 0) per_sm = 1;
     long long want = (long long)sms * per_sm;
@@ -726,12 +767,17 @@ cudaError_t launch_step(cudaStream_t s, const StepLaunch& a) {
         return a.rng_kind == 1 ? launch_chained(k_move<1>, blocks, kMoveThreads, s, a)
                                : launch_chained(k_move<0>, blocks, kMoveThreads, s, a);
     }
+    if (a.disp_max) {  // a host tick that queries the previous index (keys, one tick)
+        if (!key || !a.index_pos || a.ticks != 1) return cudaErrorInvalidValue;
+        return a.rng_kind == 1 ? launch_chained(k_step<1, true, true>, a.blocks, kStepThreads, s, a)
+                               : launch_chained(k_step<0, true, true>, a.blocks, kStepThreads, s, a);
+    }
     if (a.rng_kind == 1) {
-        return key ? launch_chained(k_step<1, true>, a.blocks, kStepThreads, s, a)
-                   : launch_chained(k_step<1, false>, a.blocks, kStepThreads, s, a);
+        return key ? launch_chained(k_step<1, true, false>, a.blocks, kStepThreads, s, a)
+                   : launch_chained(k_step<1, false, false>, a.blocks, kStepThreads, s, a);
     } else {
-        return key ? launch_chained(k_step<0, true>, a.blocks, kStepThreads, s, a)
-                   : launch_chained(k_step<0, false>, a.blocks, kStepThreads, s, a);
+        return key ? launch_chained(k_step<0, true, false>, a.blocks, kStepThreads, s, a)
+                   : launch_chained(k_step<0, false, false>, a.blocks, kStepThreads, s, a);
     }
     return cudaGetLastError();
 }
@@ -901,6 +947,19 @@ cudaError_t launch_merge(cudaStream_t s, const uint32_t* a_key, const uint32_t* 
                        static_cast<const uint32_t*>(err));
     if (e == cudaSuccess && kernels) *kernels = 3;
     return e;
+}
+
+cudaError_t launch_gather_chunk(cudaStream_t s, const uint32_t* P, uint32_t n, uint32_t lo, uint32_t cnt,
+                                const float2* pos, float2* out) {
+    if (n == 0 || cnt == 0) return cudaSuccess;
+    if (cnt > n || lo > n - cnt) return cudaErrorInvalidValue;
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const unsigned want = 8u * (unsigned)std::max(sms, 1);
+    const unsigned blocks = std::min<unsigned>(want, blocks_for(n, 256u * kGatherPer));
+    k_gather_chunk<<<blocks, 256, 0, s>>>(P, n, lo, cnt, pos, out);
+    return cudaGetLastError();
 }
 
 cudaError_t launch_iota(cudaStream_t s, uint32_t* out, uint32_t n) {

@@ -57,6 +57,12 @@ struct StepLaunch {
     uint32_t* zero_a = nullptr;
     uint32_t zero_a_words = 0;
     uint32_t* zero_b = nullptr;  // one word
+    // Largest displacement of the tick (nullptr: not measured): every moved entity's
+    // max(|x - x0|, |y - y0|) against index_pos (by slot, the positions the current
+    // index was built from) is atomically maxed into *disp_max as float bits (a
+    // non-finite displacement counts as +inf).
+    const float2* index_pos = nullptr;
+    uint32_t* disp_max = nullptr;
 };
 
 cudaError_t launch_init_entities(cudaStream_t s, const DeviceMap& m, EntityState st, uint32_t n,
@@ -115,12 +121,17 @@ cudaError_t launch_mark(cudaStream_t s, const uint32_t* P, bool identity, const 
                         uint32_t* counts, uint32_t* err, unsigned long long* changed_total = nullptr,
                         uint32_t spin_limit = kDefaultSpinLimit);
 // chunk_count_zeroed: the long-gap counter was already zeroed in the tick (else a
-// memset does it first).
+// memset does it first).  sorted_pos NULL: no positions are gathered (pos unused).
 cudaError_t launch_merge(cudaStream_t s, const uint32_t* a_key, const uint32_t* a_val, const uint32_t* b_key,
                          const uint32_t* b_val, const uint32_t* counts, uint32_t* split, uint32_t n,
                          uint32_t* out_key, uint32_t* out_val, const float2* pos, float2* sorted_pos,
                          uint32_t* kstart, uint32_t num_keys, uint4* chunks, uint32_t* chunk_count, uint32_t* err,
                          uint32_t* kernels, bool chunk_count_zeroed = false);
+// out[q] = pos[P[q]] for the q whose slot P[q] lies in [lo, lo + cnt) (q < n; the
+// other entries are left as they are): the positions of one uploaded chunk of a host
+// tick copied to their places in the sorted order P.
+cudaError_t launch_gather_chunk(cudaStream_t s, const uint32_t* P, uint32_t n, uint32_t lo, uint32_t cnt,
+                                const float2* pos, float2* out);
 cudaError_t launch_iota(cudaStream_t s, uint32_t* out, uint32_t n);
 // *first_bad = first i with (head[i] & road mask) >= num_roads, or 0xffffffff
 cudaError_t launch_check_roads(cudaStream_t s, const uint32_t* head, uint32_t n, uint32_t num_roads,

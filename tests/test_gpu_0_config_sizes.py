@@ -226,7 +226,8 @@ def test_host_tick_config_sizes(msim, orc, n, side, ticks, with_idx):
     page-locked arrays for input and output; only positions and counts downloaded,
     the changed headings and RNG states written into the arrays by the move kernel).
     16 M entities: 4 host ticks, state and counts against the oracle after each; 1 M:
-    20 host ticks, with the id lists too."""
+    20 host ticks, with the id lists too.  From the second host tick on, the query reads
+    the previous state's index with widened boxes."""
     if n > 4_000_000:
         avail = _host_available_bytes()
         if avail is not None and avail < n * 200:
@@ -259,6 +260,8 @@ def test_host_tick_config_sizes(msim, orc, n, side, ticks, with_idx):
                 if with_idx:
                     assert np.array_equal(state["idx"], i), f"neighbour lists differ {what}"
             assert sim.tick == ticks
+            # every host tick after the first queried the previous state's index (widened boxes)
+            assert sim.host_tick_stats()["skin_queries"] == ticks - 1
         finally:
             for b in bufs.values():
                 b.free()

@@ -162,3 +162,43 @@ def test_set_device_checks_its_argument(msim):
         sim.init_entities(1, placement="fraction", speed=SPEED)
         sim.step(2, neighbours=True)
         sim.sync()
+
+
+def test_host_tick_background_update_timeout(msim, orc):
+    """With consecutive neighbour host ticks the index of the new state is built after
+    the tick's query, off the caller's path; a wait of that update that gives up is
+    reported by the next call (MSIM_ERR_TIMEOUT, its moved state intact), and the host
+    ticks after it match the oracle again (the index is rebuilt by a full sort)."""
+    rm = msim.RoadMap.lattice(32, 3)
+    n, cap = 150_000, 16
+    ost = list(_oracle(orc, rm, n))
+    with msim.Simulation(rm, n, rng="pcg32", dt=0.1, radius=2.0, cap=cap, index="incremental") as sim:
+        sim.init_entities(SEED, placement="fraction", speed=SPEED)
+        state = {k: v.copy() for k, v in sim.get_state().items()}
+
+        def host_tick(what):
+            nonlocal state
+            got = sim.tick_host(state, neighbours=True, with_idx=True)
+            _advance(orc, rm, ost, 1)
+            assert np.array_equal(got["pos"].view(np.uint32), ost[0].view(np.uint32)), f"positions differ {what}"
+            ocnt, oidx, _ = orc.neighbours(ost[0], 2.0, cap, threads=8)
+            assert np.array_equal(got["count"], ocnt) and np.array_equal(got["idx"], oidx), f"neighbours differ {what}"
+            state = {"pos": got["pos"].copy(), "heading": got["heading"].copy(), "rng": got["rng"].copy(),
+                     "speed": state["speed"]}
+
+        host_tick("at the first host tick")
+        host_tick("at the second host tick")
+        assert sim.host_tick_stats()["skin_queries"] == 1
+        sim.set_wait_limit(2048)
+        sim.inject_fault(msim._capi.FAULT_SORT_TILE)  # hits the index update after this tick's query
+        host_tick("at the tick whose index update gives up")
+        with pytest.raises(msim.MsimError) as ei:
+            sim.tick_host(state, neighbours=True)
+        assert ei.value.code == 4, str(ei.value)  # MSIM_ERR_TIMEOUT
+        _advance(orc, rm, ost, 1)
+        _same_state(sim, ost, "after the call that reported the timeout")
+        sim.set_wait_limit(0)
+        state = {k: v.copy() for k, v in sim.get_state().items()}
+        for t in range(4):
+            host_tick(f"{t + 1} host ticks after recovery")
+        sim.sync()

@@ -196,3 +196,75 @@ def test_tick_host_in_place(msim, orc, pinned):
         assert np.any(rng != st["rng"])  # road-end draws happened, so the RNG write-back was exercised
         for b in bufs.values():
             b.free()
+
+
+@pytest.mark.parametrize("side,n,cap", [(48, 200_000, 16), (16, 100_000, 8)])
+@pytest.mark.parametrize("rng", ["pcg32", "xorshift128"])
+def test_skin_query_matches_oracle(msim, orc, side, n, cap, rng):
+    """Consecutive neighbour host ticks: from the second on, the query reads the index
+    of the previous state with every box widened by the tick's largest displacement,
+    and the index of the new state is built after it.  Counts and lists equal the
+    oracle's every tick.  A host edit that moves entities by 0.2 m keeps that path; one
+    that moves them by 1 m (more than a quarter of the radius) takes the usual order
+    for that tick.  (48, 200,000): tiles of about 11 m, boxes within 2 x 2 tiles; (16,
+    100,000): tiles of 2 x reach, so widened boxes span three tiles, and about 15
+    neighbours per entity, beyond the eight kept in registers.)"""
+    road_map = msim.RoadMap.lattice(side, 5)
+    rk = {"xorshift128": 0, "pcg32": 1}[rng]
+    radius = 2.0
+    rs = np.random.default_rng(side)
+    with msim.Simulation(road_map, n, rng=rng, dt=0.1, radius=radius, cap=cap, index="incremental") as sim:
+        sim.init_entities(6, placement="fraction", speed=(1.0, 1.6))
+        st = sim.get_state()
+        state = {k: st[k].copy() for k in ("pos", "heading", "rng", "speed")}
+        sim.reset_kernel_stats()
+        skin = 0
+        for t in range(10):
+            if t == 4:  # the host moves 3,000 entities by 0.2 m
+                who = rs.choice(n, 3000, replace=False)
+                state["pos"][who, 0] += np.float32(0.2)
+            if t == 7:  # and 100 by 1 m
+                who = rs.choice(n, 100, replace=False)
+                state["pos"][who, 1] -= np.float32(1.0)
+            pos, head, rng_s = state["pos"].copy(), state["heading"].copy(), state["rng"].copy()
+            got = sim.tick_host(state, neighbours=True, with_idx=True)
+            orc.step(road_map.road_pos, road_map.road_conn, road_map.connections, pos, head, rng_s, state["speed"], rk,
+                     0.1, 1, threads=8)
+            _same_state(got, {"pos": pos, "heading": head, "rng": rng_s}, f"at host tick {t + 1}")
+            ocnt, oidx, _ = orc.neighbours(pos, radius, cap, threads=8)
+            assert np.array_equal(got["count"], ocnt), f"counts differ at host tick {t + 1}"
+            assert np.array_equal(got["idx"], oidx), f"lists differ at host tick {t + 1}"
+            hs = sim.host_tick_stats()
+            if t >= 1 and t != 7:
+                skin += 1
+            assert hs["host_ticks"] == t + 1
+            assert hs["skin_queries"] == skin, (t, hs)
+            if t == 7:
+                assert hs["last_displacement"] > 0.25 * radius
+            state = {"pos": got["pos"].copy(), "heading": got["heading"].copy(), "rng": got["rng"].copy(),
+                     "speed": state["speed"]}
+        # the context's exports follow the last query (its index has moved on since)
+        cnt, idx = sim.get_neighbours()
+        assert np.array_equal(cnt, ocnt) and np.array_equal(idx, oidx)
+        assert sim.collision_pairs() == int(ocnt.sum()) // 2
+        # regular ticks on the same context, then host ticks again
+        pos, head, rng_s = state["pos"].copy(), state["heading"].copy(), state["rng"].copy()
+        for t in range(3):
+            sim.step(1, neighbours=True)
+            orc.step(road_map.road_pos, road_map.road_conn, road_map.connections, pos, head, rng_s, state["speed"], rk,
+                     0.1, 1, threads=8)
+            _same_state(sim.get_state(), {"pos": pos, "heading": head, "rng": rng_s}, f"at regular tick {t + 1}")
+            ocnt, oidx, _ = orc.neighbours(pos, radius, cap, threads=8)
+            cnt, idx = sim.get_neighbours()
+            assert np.array_equal(cnt, ocnt) and np.array_equal(idx, oidx), f"neighbours differ at regular tick {t + 1}"
+        state = {"pos": pos.copy(), "heading": head.copy(), "rng": rng_s.copy(), "speed": state["speed"]}
+        for t in range(3):
+            got = sim.tick_host(state, neighbours=True, with_idx=True)
+            orc.step(road_map.road_pos, road_map.road_conn, road_map.connections, pos, head, rng_s, state["speed"], rk,
+                     0.1, 1, threads=8)
+            _same_state(got, {"pos": pos, "heading": head, "rng": rng_s}, f"at host tick {t + 11}")
+            ocnt, oidx, _ = orc.neighbours(pos, radius, cap, threads=8)
+            assert np.array_equal(got["count"], ocnt) and np.array_equal(got["idx"], oidx)
+            state = {"pos": got["pos"].copy(), "heading": got["heading"].copy(), "rng": got["rng"].copy(),
+                     "speed": state["speed"]}
+        assert sim.host_tick_stats()["skin_queries"] == skin + 2  # the first after the regular ticks sorts
