@@ -128,11 +128,20 @@ typedef struct msim_params {
 
 /* msim_params.flags: how neighbour ticks rebuild the index (same results either way).
  * By default the previous order is updated (only entries whose key changed are
- * sorted and merged back; the first neighbour tick sorts fully).
+ * sorted and merged back; the first neighbour tick sorts fully), and between updates
+ * the index is reused: a neighbour tick queries the index built a few ticks earlier
+ * with every box widened by a bound on how far any entity can have moved since
+ * (ticks x max |speed| x max |road factor| x dt, plus rounding), and the index is
+ * updated once that bound would pass a quarter of the radius (and on the tick after
+ * the entities were set, moved by the host or re-ordered).  An entity within the
+ * radius of another now lay within radius + bound of it, in each coordinate, when
+ * the index was built, so the results are the same.
  * FULL_SORT: always a full radix sort (e.g. entities that move far between ticks);
- * INCREMENTAL: the update (the default; kept for callers that name it). */
+ * INCREMENTAL: the update (the default; kept for callers that name it);
+ * NO_REUSE: update the index on every neighbour tick (host ticks included). */
 #define MSIM_PARAM_FULL_SORT 1u
 #define MSIM_PARAM_INCREMENTAL 2u
+#define MSIM_PARAM_NO_REUSE 4u
 
 typedef struct msim_init {
     uint64_t seed;

@@ -153,7 +153,7 @@ class Simulation:
 
     def __init__(self, road_map: RoadMap, num_entities: int, *, rng: str = "xorshift128", dt: float = 1.0,
                  radius: float = 10.0, cap: int = 64, cell_size: float = 0.0, resort_interval: int = 0,
-                 index: str = "auto"):
+                 index: str = "auto", reuse: bool = True):
         self.map = road_map
         self.n = int(num_entities)
         self.cap = int(cap)
@@ -161,7 +161,8 @@ class Simulation:
         p = _capi.MsimParams(num_entities=self.n, rng_kind=self.rng_kind, dt=dt, radius=radius, cap=self.cap,
                              cell_size=cell_size, resort_interval=resort_interval,
                              flags={"auto": 0, "full": _capi.PARAM_FULL_SORT,
-                                    "incremental": _capi.PARAM_INCREMENTAL}[index])
+                                    "incremental": _capi.PARAM_INCREMENTAL}[index]
+                             | (0 if reuse else _capi.PARAM_NO_REUSE))
         self._ctx = ctypes.c_void_p()
         v = road_map.view()
         check(lib().msim_create(ctypes.byref(v), ctypes.byref(p), ctypes.byref(self._ctx)))

@@ -28,6 +28,7 @@ PLACE_UNIFORM_FRACTION = 1
 STEP_NEIGHBOURS = 1
 PARAM_FULL_SORT = 1
 PARAM_INCREMENTAL = 2
+PARAM_NO_REUSE = 4
 NO_NEIGHBOUR = 0xFFFFFFFF
 FAULT_NONE = 0
 FAULT_SORT_TILE = 1

@@ -132,12 +132,30 @@ struct msim_ctx {
     unsigned long long* sorted_dev = nullptr;
     uint64_t sorted_host = 0;
     uint64_t index_updates = 0;
-    // Host ticks that query the previous index (the skin query): index_on_state = the
-    // current index was built from the keys of the current state (slot = id, nothing
-    // moved or set since); skin_pos = the new positions in that index's sorted order;
-    // disp = the tick's largest displacement (device word, float bits); disp_host =
-    // page-locked words: [0] its copy, [1] the device status as the query left it.
-    bool index_on_state = false;
+    // Index reuse: neighbour ticks between index updates query the last index with
+    // every box widened by how far an entity can have moved since.  reuse_ticks = move
+    // ticks since the keys of the current index were computed (-1: the index does not
+    // describe the state); step_bound = bound on any entity's displacement in one tick,
+    // per coordinate (valid with bounds_valid; from max |speed|, max |road factor|, dt
+    // and the largest coordinate, for the rounding); reuse_pos = the positions of a
+    // reusing tick in the index's sorted order, alternating between ticks.
+    bool reuse = true;
+    int64_t reuse_ticks = -1;
+    bool bounds_valid = false;
+    double step_bound = 0.0;
+    double max_factor = 1.0;
+    double maxc = 0.0;
+    uint32_t* bounds_dev = nullptr;  // [max |speed|, max |coordinate|] as float bits
+    float2* reuse_pos[2] = {nullptr, nullptr};
+    cudaEvent_t ev_reuse_read[2] = {nullptr, nullptr};
+    bool reuse_read_pending[2] = {false, false};
+    int reuse_buf = 0;
+    // Host ticks: with the index built from the state they start from (reuse_ticks ==
+    // 0, slot = id), the query reads it with boxes widened by the tick's measured
+    // largest displacement (the skin query); skin_pos = the new positions in that
+    // index's sorted order; disp = that displacement (device word, float bits);
+    // disp_host = page-locked words: [0] its copy, [1] the device status as the query
+    // left it.
     bool state_free_event = false;
     uint64_t host_ticks = 0, skin_queries = 0;  // since the stats were reset
     float last_disp = 0.f;  // ev_state_free marks the last read of the spare state buffer
@@ -260,7 +278,7 @@ void free_all(msim_ctx* c) {
         if (c->ev_up[k]) cudaEventDestroy(c->ev_up[k]);
         if (c->ev_moved[k]) cudaEventDestroy(c->ev_moved[k]);
     }
-    for (cudaEvent_t e : {c->ev_disp, c->ev_query, c->ev_state_free})
+    for (cudaEvent_t e : {c->ev_disp, c->ev_query, c->ev_state_free, c->ev_reuse_read[0], c->ev_reuse_read[1]})
         if (e) cudaEventDestroy(e);
     if (c->disp_host) cudaFreeHost(c->disp_host);
     c->disp_host = nullptr;
@@ -372,6 +390,35 @@ bool ensure_skin(msim_ctx* c) {
         c->disp_host = static_cast<uint32_t*>(h);
     }
     return true;
+}
+
+// Buffers of index reuse on the device path (allocated by the first reusing tick):
+// false when an allocation fails, and the ticks then update the index every time.
+bool ensure_reuse(msim_ctx* c) {
+    for (int b = 0; b < 2; b++) {
+        if (!c->reuse_pos[b]) {
+            void* raw = nullptr;
+            if (!device_malloc(&raw, sizeof(float2) * std::max<size_t>(c->n, 1))) return false;
+            c->allocs.push_back(raw);
+            c->device_bytes += sizeof(float2) * std::max<size_t>(c->n, 1);
+            c->reuse_pos[b] = static_cast<float2*>(raw);
+        }
+        if (!c->ev_reuse_read[b] && cudaEventCreateWithFlags(&c->ev_reuse_read[b], cudaEventDisableTiming) != cudaSuccess) {
+            cudaGetLastError();
+            c->ev_reuse_read[b] = nullptr;
+            return false;
+        }
+    }
+    return true;
+}
+
+// Widened reach for queries that read an index built `ticks` move ticks ago: reach +
+// ticks * step_bound, rounded up to a float.
+float widened_reach(const msim_ctx* c, double ticks) {
+    const double r = (double)c->grid.reach + ticks * c->step_bound;
+    float rf = (float)r;
+    if ((double)rf < r) rf = std::nextafter(rf, INFINITY);
+    return rf;
 }
 
 StepLaunch step_args(msim_ctx* c, uint32_t ticks, bool key) {
@@ -518,7 +565,7 @@ int permute_state(msim_ctx* c) {
 // Forget the index (new entity state in slot = id order): the next neighbour tick
 // runs a full sort, and the one after re-orders the state by it.
 void reset_index(msim_ctx* c) {
-    c->index_on_state = false;
+    c->reuse_ticks = -1;
     c->state_free_event = false;
     c->have_nbr = false;
     c->have_sort = false;
@@ -532,7 +579,8 @@ void reset_index(msim_ctx* c) {
 // tree (random_move.comp:863-867); here: sort by tile and re-order the state.
 int build_index(msim_ctx* c) {
     c->have_nbr = false;
-    c->index_on_state = false;
+    c->reuse_ticks = -1;
+    c->bounds_valid = false;
     c->state_free_event = false;
     if (c->n == 0) return MSIM_OK;
     int rc = sort_entities(c, 0);
@@ -627,24 +675,91 @@ int key_start_table(msim_ctx* c);
 int run_query(msim_ctx* c, bool overlap, uint32_t* count_by_id = nullptr, const float2* pos = nullptr,
               const TileGrid* grid = nullptr);
 
+// Bound on any entity's displacement in one move tick, per coordinate, for index
+// reuse.  A move advances at most step = |speed| * |road factor| * dt toward its target
+// and snaps to it when closer (the rest of the step is discarded), so it moves at most
+// step; each coordinate's rounding adds at most half an ulp of the largest coordinate,
+// which no later position exceeds (every move heads for a road end, so positions stay
+// within max(largest coordinate now, largest map coordinate)).  Computed from the
+// current state (one reduction and a read-back) while the index describes it
+// (reuse_ticks == 0), so the bound covers every tick since the build.
+int ensure_bounds(msim_ctx* c) {
+    if (c->bounds_valid) return MSIM_OK;
+    CK(cudaMemsetAsync(c->bounds_dev, 0, 2 * sizeof(uint32_t), c->stream), "memset bounds");
+    CK(launch_bounds(c->stream, cur_state(c).speed, cur_state(c).pos, c->n, c->bounds_dev), "k_bounds");
+    uint32_t h[2] = {0u, 0u};
+    CK(cudaMemcpyAsync(h, c->bounds_dev, sizeof(h), cudaMemcpyDeviceToHost, c->stream), "read bounds");
+    CK(cudaStreamSynchronize(c->stream), "cudaStreamSynchronize");
+    float vmax = 0.f, cmax = 0.f;
+    std::memcpy(&vmax, &h[0], sizeof(float));
+    std::memcpy(&cmax, &h[1], sizeof(float));
+    const double step = (double)vmax * c->max_factor * (double)c->params.dt * (1.0 + 0x1p-20) +
+                        std::max((double)cmax, c->maxc) * 0x1p-22 + 1e-30;
+    c->step_bound = std::isfinite(step) ? step : INFINITY;
+    c->bounds_valid = true;
+    return MSIM_OK;
+}
+
 int neighbour_tick(msim_ctx* c) {
     NvtxRange range("msim neighbour tick");
     int rc;
     if (c->tick_timing) CK(cudaEventRecord(c->ev_tick[0], c->stream), "cudaEventRecord");
-    if (c->have_sort && c->since_permute >= c->resort) {
-        rc = permute_state(c);
-        if (rc != MSIM_OK) return rc;
+    // Index reuse: while the widened boxes of this tick stay within a quarter of the
+    // reach, the tick moves the entities, gathers their positions into the index's
+    // sorted order and queries the index built reuse_ticks + 1 ticks before; the
+    // widening costs about 1 % of the query at 16 M (reach 2 m + 0.49 m: 0.390 ms
+    // against 0.385), the update it skips (split, passes, merge) about 0.30 ms.
+    const double ticks = c->reuse_ticks >= 0 ? (double)c->reuse_ticks + 1.0 : 0.0;
+    bool reuse = false;
+    if (c->reuse && c->sorted_key && !c->order_identity && c->reuse_ticks >= 0 && c->grid.reach > 0.f &&
+        (c->bounds_valid || c->reuse_ticks == 0)) {
+        if ((rc = ensure_bounds(c)) != MSIM_OK) return rc;
+        reuse = ticks * c->step_bound <= (double)kSkinFraction * (double)c->grid.reach && ensure_reuse(c);
     }
-    if (c->sorted_key && c->incremental) {
-        rc = incremental_index(c);
-        if (rc != MSIM_OK) return rc;
-    } else {
-        rc = sort_entities(c, 1);
-        if (rc != MSIM_OK) return rc;
-        rc = key_start_table(c);
-        if (rc != MSIM_OK) return rc;
+    if (!reuse) {
+        if (c->have_sort && c->since_permute >= c->resort) {
+            rc = permute_state(c);
+            if (rc != MSIM_OK) return rc;
+        }
+        if (c->sorted_key && c->incremental) {
+            rc = incremental_index(c);
+            if (rc != MSIM_OK) return rc;
+        } else {
+            rc = sort_entities(c, 1);
+            if (rc != MSIM_OK) return rc;
+            rc = key_start_table(c);
+            if (rc != MSIM_OK) return rc;
+        }
+        rc = run_query(c, true);
+        if (rc == MSIM_OK) c->reuse_ticks = 0;
+        return rc;
     }
-    return run_query(c, true);
+    {
+        Prof p(c, K_STEP);
+        CKL(p, launch_step(c->stream, step_args(c, 1, false)), "k_step");
+    }
+    if (c->tick_timing) CK(cudaEventRecord(c->ev_tick[1], c->stream), "cudaEventRecord");
+    // the buffer the query two ticks back read (it may still run on the query stream)
+    const int x = c->reuse_buf = 1 - c->reuse_buf;
+    if (c->reuse_read_pending[x]) {
+        CK(cudaStreamWaitEvent(c->stream, c->ev_reuse_read[x], 0), "cudaStreamWaitEvent");
+        c->reuse_read_pending[x] = false;
+    }
+    {
+        Prof p(c, K_GATHER);
+        CKL(p, launch_gather_chunk(c->stream, c->sorted_slot, c->n, 0, c->n, cur_state(c).pos, c->reuse_pos[x]),
+            "k_gather_chunk");
+    }
+    TileGrid g = c->grid;
+    g.reach = widened_reach(c, ticks);
+    rc = run_query(c, true, nullptr, c->reuse_pos[x], &g);
+    if (rc != MSIM_OK) return rc;
+    if (!c->profiling) {  // the query ran on the query stream (see run_query)
+        CK(cudaEventRecord(c->ev_reuse_read[x], c->qstream), "cudaEventRecord");
+        c->reuse_read_pending[x] = true;
+    }
+    c->reuse_ticks = (int64_t)ticks;
+    return MSIM_OK;
 }
 
 // key-start table and positions in sorted order, after a full sort
@@ -750,7 +865,8 @@ int msim_create(const msim_map* map, const msim_params* params, msim_ctx** out) 
     if (!std::isfinite(p.radius) || p.radius < 0.f) return fail(MSIM_ERR_INVALID, "radius must be finite and >= 0");
     if (p.cap > kMaxCap) return fail(MSIM_ERR_INVALID, "cap must be <= " + std::to_string(kMaxCap));
     if (p.cell_size < 0.f || !std::isfinite(p.cell_size)) return fail(MSIM_ERR_INVALID, "cell_size must be >= 0");
-    if (p.flags & ~(MSIM_PARAM_FULL_SORT | MSIM_PARAM_INCREMENTAL)) return fail(MSIM_ERR_INVALID, "unknown params flags");
+    if (p.flags & ~(MSIM_PARAM_FULL_SORT | MSIM_PARAM_INCREMENTAL | MSIM_PARAM_NO_REUSE))
+        return fail(MSIM_ERR_INVALID, "unknown params flags");
     if ((p.flags & MSIM_PARAM_FULL_SORT) && (p.flags & MSIM_PARAM_INCREMENTAL))
         return fail(MSIM_ERR_INVALID, "MSIM_PARAM_FULL_SORT and MSIM_PARAM_INCREMENTAL exclude each other");
 
@@ -766,6 +882,7 @@ int msim_create(const msim_map* map, const msim_params* params, msim_ctx** out) 
     // 250 K, 1 M and 16 M entities at the lattice density: 0.051 against 0.060 ms per
     // tick at 62.5 K, 0.092 against 0.114 at 1 M)
     c->incremental = (p.flags & MSIM_PARAM_FULL_SORT) == 0;
+    c->reuse = (p.flags & MSIM_PARAM_NO_REUSE) == 0;
     c->n = p.num_entities;
     c->R = map->num_roads;
     c->C = map->num_connections;
@@ -792,6 +909,7 @@ int msim_create(const msim_map* map, const msim_params* params, msim_ctx** out) 
     const double radius = p.radius;
     // reach covers the rounding of |dx| in the predicate and of pos -/+ reach
     const double reach = radius * (1.0 + 0x1p-20) + maxc * 0x1p-20 + 1e-30;
+    c->maxc = maxc;
     double cell = p.cell_size;
     if (cell <= 0.0) {
         // about four entities per tile at uniform density (entities on roads bunch up
@@ -858,7 +976,7 @@ int msim_create(const msim_map* map, const msim_params* params, msim_ctx** out) 
         (rc = dalloc(c, &c->b_val[1], n)) || (rc = dalloc(c, &c->ab_counts, 2)) ||
         (rc = dalloc(c, &c->merge_split, (size_t)merge_tiles(c->n) + 1)) || (rc = dalloc(c, &c->sorted_dev, 1)) ||
         (rc = dalloc(c, &c->nbr_count, n)) || (rc = dalloc(c, &c->pairs, kPairBins)) || (rc = dalloc(c, &c->err, 1)) ||
-        (rc = dalloc(c, &c->check, 1)))
+        (rc = dalloc(c, &c->check, 1)) || (rc = dalloc(c, &c->bounds_dev, 2)))
         return bail(rc);
     for (int b = 0; b < 2; b++) {
         if ((rc = dalloc(c, &c->kstart_b[b], c->num_keys + 1)) ||
@@ -968,6 +1086,7 @@ int msim_set_entities(msim_ctx* c, const float* pos, const uint32_t* heading, co
     // pays it).
     CK(launch_iota(c->stream, s.slot_id, c->n), "k_iota");
     reset_index(c);
+    c->bounds_valid = false;
     c->slots_identity = true;
     return MSIM_OK;
 }
@@ -976,11 +1095,18 @@ int msim_set_road_factors(msim_ctx* c, const float* factors) {
     int rc = check_ctx(c);
     if (rc != MSIM_OK) return rc;
     if (!factors) return fail(MSIM_ERR_INVALID, "factors is NULL");
-    for (uint32_t r = 0; r < c->R; r++)
+    double fmax = 0.0;
+    for (uint32_t r = 0; r < c->R; r++) {
         if (!std::isfinite(factors[r])) return fail(MSIM_ERR_INVALID, "non-finite road factor");
+        fmax = std::max(fmax, std::fabs((double)factors[r]));
+    }
     if (!c->factor && (rc = dalloc(c, &c->factor, c->R))) return rc;
     CK(cudaMemcpyAsync(c->factor, factors, sizeof(float) * c->R, cudaMemcpyHostToDevice, c->stream), "upload factors");
     CK(cudaStreamSynchronize(c->stream), "sync");
+    // ticks from here on move by the new factors: an index built before is not reused
+    c->max_factor = fmax;
+    c->bounds_valid = false;
+    if (c->reuse_ticks > 0) c->reuse_ticks = -1;
     return MSIM_OK;
 }
 
@@ -993,7 +1119,6 @@ int msim_step(msim_ctx* c, uint32_t ticks, uint32_t flags) {
         c->tick += ticks;
         return MSIM_OK;
     }
-    c->index_on_state = false;  // (a neighbour tick may also re-order the state)
     c->state_free_event = false;
     if (flags & MSIM_STEP_NEIGHBOURS) {
         for (uint32_t t = 0; t < ticks; t++) {
@@ -1018,6 +1143,7 @@ int msim_step(msim_ctx* c, uint32_t ticks, uint32_t flags) {
         CKL(p, launch_step(c->stream, step_args(c, t, false)), "k_step_multi");
         left -= t;
         c->tick += t;
+        if (c->reuse_ticks >= 0) c->reuse_ticks += t;  // moved without an index update
     }
     return MSIM_OK;
 }
@@ -1127,8 +1253,9 @@ int msim_tick_host(msim_ctx* c, const float* in_pos, const uint32_t* in_heading,
     // uploads.  A d above a quarter of the reach (host edits between ticks, large
     // steps) takes the usual order: index update, then query.
     const bool state_free_event = c->state_free_event;
-    bool skin = use_inc && c->index_on_state && c->grid.reach > 0.f && ensure_skin(c);
-    c->index_on_state = false;
+    bool skin = c->reuse && use_inc && c->reuse_ticks == 0 && c->grid.reach > 0.f && ensure_skin(c);
+    c->reuse_ticks = -1;
+    c->bounds_valid = false;  // speeds and positions come from the host
     c->state_free_event = false;
     // In place (the same page-locked arrays for heading and RNG in and out): they
     // already hold every value the tick leaves unchanged, so the move kernel writes the
@@ -1330,7 +1457,7 @@ int msim_tick_host(msim_ctx* c, const float* in_pos, const uint32_t* in_heading,
         // a status raised before the query (e.g. by the previous call's index update):
         // reported now, after everything on the context's stream
         if (status) return sync_and_check(c);
-        c->index_on_state = true;
+        c->reuse_ticks = 0;
         c->state_free_event = true;
         c->host_ticks++;
         c->skin_queries++;
@@ -1338,7 +1465,7 @@ int msim_tick_host(msim_ctx* c, const float* in_pos, const uint32_t* in_heading,
     }
     rc = sync_and_check(c);
     if (rc == MSIM_OK) {
-        c->index_on_state = nbr;  // the index was built from this state
+        c->reuse_ticks = nbr ? 0 : -1;  // the index was built from this state
         c->host_ticks++;
     }
     return rc;

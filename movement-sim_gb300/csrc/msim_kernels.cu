@@ -707,6 +707,35 @@ __global__ __launch_bounds__(256) void k_gather_chunk(const uint32_t* __restrict
     }
 }
 
+__device__ __forceinline__ uint32_t abs_bits(float v) {  // |v| as ordered bits; NaN / inf: +inf
+    const float a = fabsf(v);
+    return a <= 3.0e38f ? __float_as_uint(a) : 0x7f800000u;
+}
+
+__global__ __launch_bounds__(256) void k_bounds(const float* __restrict__ speed, const float2* __restrict__ pos,
+                                                uint32_t n, uint32_t* out) {
+    __shared__ uint32_t s_max[2];
+    if (threadIdx.x == 0) s_max[0] = s_max[1] = 0u;
+    __syncthreads();
+    uint32_t ms = 0u, mp = 0u;
+    for (uint32_t i = blockIdx.x * 256u + threadIdx.x; i < n; i += gridDim.x * 256u) {
+        const float2 p = pos[i];
+        ms = max(ms, abs_bits(speed[i]));
+        mp = max(mp, max(abs_bits(p.x), abs_bits(p.y)));
+    }
+    ms = __reduce_max_sync(0xffffffffu, ms);
+    mp = __reduce_max_sync(0xffffffffu, mp);
+    if ((threadIdx.x & 31u) == 0) {
+        atomicMax(&s_max[0], ms);
+        atomicMax(&s_max[1], mp);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        atomicMax(&out[0], s_max[0]);
+        atomicMax(&out[1], s_max[1]);
+    }
+}
+
 __global__ void k_iota(uint32_t* out, uint32_t n) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) out[i] = i;
@@ -959,6 +988,16 @@ cudaError_t launch_gather_chunk(cudaStream_t s, const uint32_t* P, uint32_t n, u
     const unsigned want = 8u * (unsigned)std::max(sms, 1);
     const unsigned blocks = std::min<unsigned>(want, blocks_for(n, 256u * kGatherPer));
     k_gather_chunk<<<blocks, 256, 0, s>>>(P, n, lo, cnt, pos, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_bounds(cudaStream_t s, const float* speed, const float2* pos, uint32_t n, uint32_t* out) {
+    if (n == 0) return cudaSuccess;
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const unsigned blocks = std::min<unsigned>(8u * (unsigned)std::max(sms, 1), blocks_for(n, 256u));
+    k_bounds<<<blocks, 256, 0, s>>>(speed, pos, n, out);
     return cudaGetLastError();
 }
 

@@ -132,6 +132,9 @@ cudaError_t launch_merge(cudaStream_t s, const uint32_t* a_key, const uint32_t* 
 // tick copied to their places in the sorted order P.
 cudaError_t launch_gather_chunk(cudaStream_t s, const uint32_t* P, uint32_t n, uint32_t lo, uint32_t cnt,
                                 const float2* pos, float2* out);
+// out[0] = largest |speed|, out[1] = largest |x| or |y| of the n entities, as float
+// bits (atomically maxed: out must hold zeros; NaN or infinite values count as +inf).
+cudaError_t launch_bounds(cudaStream_t s, const float* speed, const float2* pos, uint32_t n, uint32_t* out);
 cudaError_t launch_iota(cudaStream_t s, uint32_t* out, uint32_t n);
 // *first_bad = first i with (head[i] & road mask) >= num_roads, or 0xffffffff
 cudaError_t launch_check_roads(cudaStream_t s, const uint32_t* head, uint32_t n, uint32_t num_roads,

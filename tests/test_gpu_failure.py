@@ -49,11 +49,13 @@ def _same_neighbours(sim, orc, ost, cap, what):
 @pytest.mark.parametrize("index", ["full", "auto"])
 def test_wait_timeout_reports_and_recovers(msim, orc, index):
     """full: the first radix pass of a full sort; auto: the split of an incremental
-    update (both chains have 8 tiles at 30,000 entities)."""
+    update (both chains have 8 tiles at 30,000 entities).  Index reuse off, so every
+    neighbour tick updates the index (the next test covers it on)."""
     rm = msim.RoadMap.lattice(32, 3)
     n, cap = 30_000, 16
     ost = _oracle(orc, rm, n)
-    with msim.Simulation(rm, n, rng="pcg32", dt=0.1, radius=2.0, cap=cap, index=index, resort_interval=4) as sim:
+    with msim.Simulation(rm, n, rng="pcg32", dt=0.1, radius=2.0, cap=cap, index=index, resort_interval=4,
+                         reuse=False) as sim:
         sim.init_entities(SEED, placement="fraction", speed=SPEED)
         sim.step(2, neighbours=True)
         _advance(orc, rm, ost, 2)
@@ -75,14 +77,54 @@ def test_wait_timeout_reports_and_recovers(msim, orc, index):
         sim.sync()
 
 
-@pytest.mark.parametrize("arg", [0, 1, 2, 4, 7])
-def test_injected_launch_failure(msim, orc, arg):
+def test_wait_timeout_with_index_reuse(msim, orc):
+    """With index reuse the armed fault waits for the next index update (ticks that
+    reuse the index run none); that tick's wait gives up, msim_sync reports it, the
+    state is intact, and the ticks after match the oracle again."""
+    rm = msim.RoadMap.lattice(32, 3)
+    n, cap = 30_000, 16
+    ost = _oracle(orc, rm, n)
+    with msim.Simulation(rm, n, rng="pcg32", dt=0.1, radius=2.0, cap=cap, resort_interval=4) as sim:
+        sim.init_entities(SEED, placement="fraction", speed=SPEED)
+        sim.step(3, neighbours=True)
+        _advance(orc, rm, ost, 3)
+        _same_neighbours(sim, orc, ost, cap, "before the fault")
+        updates = sim.sort_stats()["index_updates"]
+        sim.set_wait_limit(2048)
+        sim.inject_fault(msim._capi.FAULT_SORT_TILE)
+        for t in range(12):  # until the tick that updates the index
+            sim.step(1, neighbours=True)
+            _advance(orc, rm, ost, 1)
+            if sim.sort_stats()["index_updates"] > updates:
+                break
+            _same_state(sim, ost, f"{t + 1} ticks after arming")
+            _same_neighbours(sim, orc, ost, cap, f"{t + 1} ticks after arming (index reused)")
+        else:
+            raise AssertionError("no index update within 12 ticks")
+        assert t >= 1  # at least one tick reused the index before
+        with pytest.raises(msim.MsimError) as ei:
+            sim.sync()
+        assert ei.value.code == 4, str(ei.value)  # MSIM_ERR_TIMEOUT
+        _same_state(sim, ost, "after the timed-out tick")
+        sim.set_wait_limit(0)
+        for t in range(8):
+            sim.step(1, neighbours=True)
+            _advance(orc, rm, ost, 1)
+            _same_state(sim, ost, f"{t + 1} ticks after recovery")
+            _same_neighbours(sim, orc, ost, cap, f"{t + 1} ticks after recovery")
+        sim.sync()
+
+
+@pytest.mark.parametrize("reuse,arg", [(False, 0), (False, 1), (False, 2), (False, 4), (False, 7),
+                                       (True, 0), (True, 1), (True, 2), (True, 5)])
+def test_injected_launch_failure(msim, orc, reuse, arg):
     """The (arg+1)-th launch of a 2-tick neighbour step fails on the host; the caller
-    restores its state with msim_set_entities and continues bit-exact."""
+    restores its state with msim_set_entities and continues bit-exact.  Without index
+    reuse both ticks update the index; with it both reuse it (move, gather, query)."""
     rm = msim.RoadMap.lattice(32, 4)
     n, cap = 20_000, 16
     ost = _oracle(orc, rm, n)
-    with msim.Simulation(rm, n, rng="pcg32", dt=0.1, radius=2.0, cap=cap) as sim:
+    with msim.Simulation(rm, n, rng="pcg32", dt=0.1, radius=2.0, cap=cap, reuse=reuse) as sim:
         sim.init_entities(SEED, placement="fraction", speed=SPEED)
         sim.step(1, neighbours=True)
         _advance(orc, rm, ost, 1)
