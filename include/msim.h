@@ -132,7 +132,7 @@ typedef struct msim_params {
  * the index is reused: a neighbour tick queries the index built a few ticks earlier
  * with every box widened by a bound on how far any entity can have moved since
  * (ticks x max |speed| x max |road factor| x dt, plus rounding), and the index is
- * updated once that bound would pass a quarter of the radius (and on the tick after
+ * updated once that bound would pass the radius (and on the tick after
  * the entities were set, moved by the host or re-ordered).  An entity within the
  * radius of another now lay within radius + bound of it, in each coordinate, when
  * the index was built, so the results are the same.
@@ -228,7 +228,7 @@ int msim_get_neighbours(msim_ctx* ctx, uint32_t* count, uint32_t* idx);
  * coordinate, when that index was built), so the neighbour results are the same; the
  * index of the new state is then built after the query, while the counts download
  * and the next call's uploads run, and a device status it raises is reported by the
- * next call.  A d above a quarter of the radius (large steps, host edits that move
+ * next call.  A d above the radius (large steps, host edits that move
  * entities) takes the usual order for that tick.  With page-locked host
  * buffers (msim_host_alloc) the copies run asynchronously; pageable ones work too.
  * in_speed may be NULL (1.4 m per tick at dt = 1); any output may be NULL; out_count

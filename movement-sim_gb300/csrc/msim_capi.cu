@@ -358,10 +358,15 @@ int ensure_stage(msim_ctx* c, size_t bytes) {
 
 EntityState& cur_state(msim_ctx* c) { return c->st[c->cur]; }
 
-// Skin query of a host tick: allowed while the tick's largest displacement is at most
-// this fraction of the reach (the boxes grow by it; at the 16 M workload d is about
-// 0.16 m against a reach of 2 m).
-constexpr float kSkinFraction = 0.25f;
+// Widened queries (index reuse on neighbour ticks, the skin query of host ticks) are
+// allowed while the widening is at most this fraction of the reach.  At the 16 M
+// workload a tick moves an entity at most 0.16 m against a reach of 2 m, and the
+// query costs about the same at any widening up to 2 m (tiles of 25.6 m, bands of
+// 6.4 m: 0.385-0.400 ms); per tick with reuse, measured at 16 M / 1 M: 0.25 of the
+// reach 0.616 / 0.0521 ms, 0.5 0.573 / 0.0473, 1.0 0.555 / 0.0447, 1.5 0.569 /
+// 0.0437, 2.0 0.558 / 0.0437, 3.0 0.568 / 0.0437.  At densities where a query meets
+// 17 or 70 neighbours it costs the same at 0 and 1.0 (1.41 and 22.4 ms at 1 M).
+constexpr float kWidenLimit = 1.0f;
 
 // Buffers of the skin query (allocated by the first host tick that can use it): false
 // when an allocation fails, and the tick then takes the usual order.
@@ -704,17 +709,17 @@ int neighbour_tick(msim_ctx* c) {
     NvtxRange range("msim neighbour tick");
     int rc;
     if (c->tick_timing) CK(cudaEventRecord(c->ev_tick[0], c->stream), "cudaEventRecord");
-    // Index reuse: while the widened boxes of this tick stay within a quarter of the
-    // reach, the tick moves the entities, gathers their positions into the index's
+    // Index reuse: while the widening of this tick's boxes stays within kWidenLimit of
+    // the reach, the tick moves the entities, gathers their positions into the index's
     // sorted order and queries the index built reuse_ticks + 1 ticks before; the
-    // widening costs about 1 % of the query at 16 M (reach 2 m + 0.49 m: 0.390 ms
-    // against 0.385), the update it skips (split, passes, merge) about 0.30 ms.
+    // widening costs little of the query (16 M, reach 2 m + 0.49 m: 0.390 ms against
+    // 0.385), the update it skips (split, passes, merge) about 0.30 ms.
     const double ticks = c->reuse_ticks >= 0 ? (double)c->reuse_ticks + 1.0 : 0.0;
     bool reuse = false;
     if (c->reuse && c->sorted_key && !c->order_identity && c->reuse_ticks >= 0 && c->grid.reach > 0.f &&
         (c->bounds_valid || c->reuse_ticks == 0)) {
         if ((rc = ensure_bounds(c)) != MSIM_OK) return rc;
-        reuse = ticks * c->step_bound <= (double)kSkinFraction * (double)c->grid.reach && ensure_reuse(c);
+        reuse = ticks * c->step_bound <= (double)kWidenLimit * (double)c->grid.reach && ensure_reuse(c);
     }
     if (!reuse) {
         if (c->have_sort && c->since_permute >= c->resort) {
@@ -1250,7 +1255,7 @@ int msim_tick_host(msim_ctx* c, const float* in_pos, const uint32_t* in_heading,
     // coordinate).  The move measures d; the new positions are gathered into the
     // index's order chunk by chunk behind the uploads; the index update for the new
     // state then runs after the query, beside the downloads and the next call's
-    // uploads.  A d above a quarter of the reach (host edits between ticks, large
+    // uploads.  A d above kWidenLimit of the reach (host edits between ticks, large
     // steps) takes the usual order: index update, then query.
     const bool state_free_event = c->state_free_event;
     bool skin = c->reuse && use_inc && c->reuse_ticks == 0 && c->grid.reach > 0.f && ensure_skin(c);
@@ -1370,7 +1375,7 @@ int msim_tick_host(msim_ctx* c, const float* in_pos, const uint32_t* in_heading,
         float d = 0.f;
         std::memcpy(&d, c->disp_host, sizeof(d));
         c->last_disp = d;
-        skin = d <= kSkinFraction * c->grid.reach;  // false for +inf (a non-finite position)
+        skin = d <= kWidenLimit * c->grid.reach;  // false for +inf (a non-finite position)
         if (skin) {
             // widened reach, rounded up: the displacement was measured with one rounding
             const double r = (double)c->grid.reach + (double)d * (1.0 + 0x1p-20);

@@ -1,8 +1,10 @@
 """Parity of the timed path at the workload sizes, against the CPU oracle.
 
 The path under test is the one the benchmark times: the incremental index update,
-the query of tick t running on a second stream beside tick t+1's move and index
-update (double-buffered index), and the re-ordering of the state every 64 ticks.
+index reuse between updates (queries on the last index with widened boxes), the
+query of tick t running on a second stream beside tick t+1's move and index update
+(double-buffered index), and the re-ordering of the state at the first index update
+after every 64 ticks.
 
 * 1,000,000 entities on the 256 x 256 lattice, radius 2 m, cap 64, all 500 ticks:
   positions, headings, RNG states, neighbour counts and id lists compared after
@@ -12,8 +14,8 @@ update (double-buffered index), and the re-ordering of the state every 64 ticks.
   tick inside a call), compared at every call boundary, with the default
   re-ordering interval and with a re-ordering every 5 ticks.
 * 16,000,000 entities on the 1024 x 1024 lattice for 135 ticks in multi-tick
-  calls: two re-orderings (before ticks 65 and 129) run under the overlap; full
-  state, counts and id lists compared just after each and at the end.
+  calls: two re-orderings run under the overlap; full state, counts and id lists
+  compared after ticks 65, 129 and 135.
 
 Integer state and id lists must be equal; positions bit for bit (tolerance 0 m).
 This file sorts first among the GPU tests so that these runs happen even when a
@@ -128,8 +130,9 @@ def test_neighbours_config_multi_tick_calls(msim, orc, resort):
 
 def test_scale_config_reorders_under_overlap(msim, orc):
     """16 M entities, 1024 x 1024 lattice: 135 ticks in three multi-tick calls;
-    the re-orderings before ticks 65 and 129 run inside the calls.  Full state,
-    counts and id lists compared after ticks 65, 129 and 135."""
+    the two re-orderings (at the first index update after 64 ticks each) run inside
+    the calls.  Full state, counts and id lists compared after ticks 65, 129 and
+    135."""
     n = 16_000_000
     avail = _host_available_bytes()
     need = n * (2 * 4 * CAP + 64)  # two id-list arrays, states and counts

@@ -92,7 +92,7 @@ def test_wait_timeout_with_index_reuse(msim, orc):
         updates = sim.sort_stats()["index_updates"]
         sim.set_wait_limit(2048)
         sim.inject_fault(msim._capi.FAULT_SORT_TILE)
-        for t in range(12):  # until the tick that updates the index
+        for t in range(24):  # until the tick that updates the index
             sim.step(1, neighbours=True)
             _advance(orc, rm, ost, 1)
             if sim.sort_stats()["index_updates"] > updates:
@@ -100,7 +100,7 @@ def test_wait_timeout_with_index_reuse(msim, orc):
             _same_state(sim, ost, f"{t + 1} ticks after arming")
             _same_neighbours(sim, orc, ost, cap, f"{t + 1} ticks after arming (index reused)")
         else:
-            raise AssertionError("no index update within 12 ticks")
+            raise AssertionError("no index update within 24 ticks")
         assert t >= 1  # at least one tick reused the index before
         with pytest.raises(msim.MsimError) as ei:
             sim.sync()

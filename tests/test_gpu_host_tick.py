@@ -204,9 +204,9 @@ def test_skin_query_matches_oracle(msim, orc, side, n, cap, rng):
     """Consecutive neighbour host ticks: from the second on, the query reads the index
     of the previous state with every box widened by the tick's largest displacement,
     and the index of the new state is built after it.  Counts and lists equal the
-    oracle's every tick.  A host edit that moves entities by 0.2 m keeps that path; one
-    that moves them by 1 m (more than a quarter of the radius) takes the usual order
-    for that tick.  (48, 200,000): tiles of about 11 m, boxes within 2 x 2 tiles; (16,
+    oracle's every tick.  A host edit that moves entities by 1.5 m keeps that path
+    (boxes widened by up to 1.66 m); one that moves them by 3 m (more than the radius)
+    takes the usual order for that tick.  (48, 200,000): tiles of about 11 m, boxes within 2 x 2 tiles; (16,
     100,000): tiles of 2 x reach, so widened boxes span three tiles, and about 15
     neighbours per entity, beyond the eight kept in registers.)"""
     road_map = msim.RoadMap.lattice(side, 5)
@@ -220,12 +220,12 @@ def test_skin_query_matches_oracle(msim, orc, side, n, cap, rng):
         sim.reset_kernel_stats()
         skin = 0
         for t in range(10):
-            if t == 4:  # the host moves 3,000 entities by 0.2 m
+            if t == 4:  # the host moves 3,000 entities by 1.5 m
                 who = rs.choice(n, 3000, replace=False)
-                state["pos"][who, 0] += np.float32(0.2)
-            if t == 7:  # and 100 by 1 m
+                state["pos"][who, 0] += np.float32(1.5)
+            if t == 7:  # and 100 by 3 m
                 who = rs.choice(n, 100, replace=False)
-                state["pos"][who, 1] -= np.float32(1.0)
+                state["pos"][who, 1] -= np.float32(3.0)
             pos, head, rng_s = state["pos"].copy(), state["heading"].copy(), state["rng"].copy()
             got = sim.tick_host(state, neighbours=True, with_idx=True)
             orc.step(road_map.road_pos, road_map.road_conn, road_map.connections, pos, head, rng_s, state["speed"], rk,
@@ -239,8 +239,10 @@ def test_skin_query_matches_oracle(msim, orc, side, n, cap, rng):
                 skin += 1
             assert hs["host_ticks"] == t + 1
             assert hs["skin_queries"] == skin, (t, hs)
+            if t == 4:
+                assert 1.3 < hs["last_displacement"] <= radius
             if t == 7:
-                assert hs["last_displacement"] > 0.25 * radius
+                assert hs["last_displacement"] > radius
             state = {"pos": got["pos"].copy(), "heading": got["heading"].copy(), "rng": got["rng"].copy(),
                      "speed": state["speed"]}
         # the context's exports follow the last query (its index has moved on since)

@@ -73,11 +73,11 @@ def test_reuse_matches_oracle_every_tick(msim, orc, side, n, cap, rng):
 
 
 def test_reuse_off_when_steps_are_large(msim, orc):
-    """Reference mode (dt = 1, 1.4 m per tick) with a 2 m radius: the bound passes a
-    quarter of the radius after one tick, so every neighbour tick updates the index."""
+    """Reference mode (dt = 1, 1.4 m per tick) with a 1 m radius: the bound passes
+    the radius after one tick, so every neighbour tick updates the index."""
     road_map = msim.RoadMap.lattice(32, 2)
     n = 30_000
-    with msim.Simulation(road_map, n, rng="xorshift128", dt=1.0, radius=2.0, cap=8) as sim:
+    with msim.Simulation(road_map, n, rng="xorshift128", dt=1.0, radius=1.0, cap=8) as sim:
         sim.init_entities(5, placement="fraction", speed=(1.4, 1.4))
         st = sim.get_state()
         ost = [st["pos"].copy(), st["heading"].copy(), st["rng"].copy(), st["speed"].copy()]
@@ -87,6 +87,6 @@ def test_reuse_off_when_steps_are_large(msim, orc):
             orc.step(road_map.road_pos, road_map.road_conn, road_map.connections, ost[0], ost[1], ost[2], ost[3], 0,
                      1.0, 1, threads=8)
             cnt, idx = sim.get_neighbours()
-            ocnt, oidx, _ = orc.neighbours(ost[0], 2.0, 8, threads=8)
+            ocnt, oidx, _ = orc.neighbours(ost[0], 1.0, 8, threads=8)
             assert np.array_equal(cnt, ocnt) and np.array_equal(idx, oidx), f"neighbours differ at tick {t + 1}"
         assert sim.sort_stats()["index_updates"] - u0 == 6
