@@ -147,6 +147,11 @@ struct msim_ctx {
     double maxc = 0.0;
     uint32_t* bounds_dev = nullptr;  // [max |speed|, max |coordinate|] as float bits
     float2* reuse_pos[2] = {nullptr, nullptr};
+    // rank[slot] = sorted position of the slot in the current index, written by the
+    // merge once allocated (rank_valid: it describes the current index); a reusing
+    // tick's move then writes each position there itself (no gather pass)
+    uint32_t* rank = nullptr;
+    bool rank_valid = false;
     cudaEvent_t ev_reuse_read[2] = {nullptr, nullptr};
     bool reuse_read_pending[2] = {false, false};
     int reuse_buf = 0;
@@ -400,6 +405,14 @@ bool ensure_skin(msim_ctx* c) {
 // Buffers of index reuse on the device path (allocated by the first reusing tick):
 // false when an allocation fails, and the ticks then update the index every time.
 bool ensure_reuse(msim_ctx* c) {
+    if (!c->rank) {
+        void* raw = nullptr;
+        if (!device_malloc(&raw, sizeof(uint32_t) * std::max<size_t>(c->n, 1))) return false;
+        c->allocs.push_back(raw);
+        c->device_bytes += sizeof(uint32_t) * std::max<size_t>(c->n, 1);
+        c->rank = static_cast<uint32_t*>(raw);
+        c->rank_valid = false;
+    }
     for (int b = 0; b < 2; b++) {
         if (!c->reuse_pos[b]) {
             void* raw = nullptr;
@@ -547,6 +560,7 @@ int sort_keys(msim_ctx* c) {
     c->chain_broken = false;
     c->sorted_key = c->sk[(c->passes - 1) & 1];
     c->sorted_slot = c->sv[(c->passes - 1) & 1];
+    c->rank_valid = false;  // a full sort writes no ranks
     c->have_sort = true;
     c->sorted_host += c->n;
     c->index_updates++;
@@ -563,6 +577,7 @@ int permute_state(msim_ctx* c) {
     c->have_sort = false;
     c->order_identity = true;  // slot q now holds the entity at sorted position q
     c->slots_identity = false;
+    c->rank_valid = false;
     c->since_permute = 0;
     return MSIM_OK;
 }
@@ -571,6 +586,7 @@ int permute_state(msim_ctx* c) {
 // runs a full sort, and the one after re-orders the state by it.
 void reset_index(msim_ctx* c) {
     c->reuse_ticks = -1;
+    c->rank_valid = false;
     c->state_free_event = false;
     c->have_nbr = false;
     c->have_sort = false;
@@ -664,8 +680,9 @@ int incremental_update(msim_ctx* c, bool positions) {
                         c->ab_counts, c->merge_split, c->n, c->sk[out], c->sv[out],
                         positions ? cur_state(c).pos : nullptr, positions ? c->sorted_pos : nullptr,
                         c->kstart, (uint32_t)c->num_keys, c->kstart_chunks, c->kstart_chunk_count, c->err,
-                        &launched, c->chunk_count_zeroed),
+                        &launched, c->chunk_count_zeroed, c->rank),
            "k_merge");
+        c->rank_valid = c->rank != nullptr;
         c->chunk_count_zeroed = false;
         if (launched > 1) c->launch_count += launched - 1;
     }
@@ -726,6 +743,7 @@ int neighbour_tick(msim_ctx* c) {
             rc = permute_state(c);
             if (rc != MSIM_OK) return rc;
         }
+        if (c->reuse) ensure_reuse(c);  // so this update writes the ranks the next ticks use
         if (c->sorted_key && c->incremental) {
             rc = incremental_index(c);
             if (rc != MSIM_OK) return rc;
@@ -739,18 +757,23 @@ int neighbour_tick(msim_ctx* c) {
         if (rc == MSIM_OK) c->reuse_ticks = 0;
         return rc;
     }
-    {
-        Prof p(c, K_STEP);
-        CKL(p, launch_step(c->stream, step_args(c, 1, false)), "k_step");
-    }
-    if (c->tick_timing) CK(cudaEventRecord(c->ev_tick[1], c->stream), "cudaEventRecord");
     // the buffer the query two ticks back read (it may still run on the query stream)
     const int x = c->reuse_buf = 1 - c->reuse_buf;
     if (c->reuse_read_pending[x]) {
         CK(cudaStreamWaitEvent(c->stream, c->ev_reuse_read[x], 0), "cudaStreamWaitEvent");
         c->reuse_read_pending[x] = false;
     }
-    {
+    {  // the move writes each position at its sorted position too, when the ranks are known
+        Prof p(c, K_STEP);
+        StepLaunch a = step_args(c, 1, false);
+        if (c->rank_valid) {
+            a.rank = c->rank;
+            a.rank_pos = c->reuse_pos[x];
+        }
+        CKL(p, launch_step(c->stream, a), "k_step");
+    }
+    if (c->tick_timing) CK(cudaEventRecord(c->ev_tick[1], c->stream), "cudaEventRecord");
+    if (!c->rank_valid) {
         Prof p(c, K_GATHER);
         CKL(p, launch_gather_chunk(c->stream, c->sorted_slot, c->n, 0, c->n, cur_state(c).pos, c->reuse_pos[x]),
             "k_gather_chunk");

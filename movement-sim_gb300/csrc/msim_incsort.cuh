@@ -247,7 +247,7 @@ __global__ __launch_bounds__(kMergeThreads, 8) void k_merge(
     const uint32_t* __restrict__ b_val, const uint32_t* __restrict__ counts, const uint32_t* __restrict__ split,
     uint32_t n, uint32_t* __restrict__ out_key, uint32_t* __restrict__ out_val, const float2* __restrict__ pos,
     float2* __restrict__ sorted_pos, uint32_t* __restrict__ kstart, uint32_t num_keys, uint4* __restrict__ chunks,
-    uint32_t* chunk_count, uint32_t chunk_cap, uint32_t* err) {
+    uint32_t* chunk_count, uint32_t chunk_cap, uint32_t* err, uint32_t* __restrict__ rank) {
     __shared__ uint32_t s_ink[kMergeTile], s_inv[kMergeTile];    // A segment, then B segment
     __shared__ uint32_t s_outk[kMergeTile], s_outv[kMergeTile];
     __shared__ uint32_t s_prev;  // clamped key of the entry before the tile
@@ -360,6 +360,13 @@ __global__ __launch_bounds__(kMergeThreads, 8) void k_merge(
                 out_key[d0 + i] = s_outk[i];
                 out_val[d0 + i] = s_outv[i];
             }
+        }
+    }
+    if (rank) {  // sorted position of every slot (ticks that reuse this index place their moves)
+#pragma unroll
+        for (uint32_t k = 0; k < kPer; k++) {
+            const uint32_t i = k * kMergeThreads + tid;
+            if (i < cnt && s_outv[i] < n) rank[s_outv[i]] = d0 + i;
         }
     }
     // Key-start entries: position p owns the entries (key[p-1], key[p]], so the kPer

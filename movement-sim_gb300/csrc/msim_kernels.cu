@@ -184,6 +184,10 @@ __global__ __launch_bounds__(kMoveThreads) void k_move(StepLaunch a) {
         a.st.pos[s] = p;
         if (h != h0) a.st.head[s] = h;
         if (rd) a.st.rng[s] = r;
+        if (a.rank_pos) {  // uniform: a tick that reuses the index
+            const uint32_t q = a.rank[s];
+            if (q < a.n) a.rank_pos[q] = p;
+        }
     }
 }
 
@@ -788,6 +792,7 @@ cudaError_t launch_init_entities(cudaStream_t s, const DeviceMap& m, EntityState
 cudaError_t launch_step(cudaStream_t s, const StepLaunch& a) {
     if (a.n == 0) return cudaSuccess;
     const bool key = a.key != nullptr;
+    if (a.rank_pos && (key || a.ticks != 1 || !a.rank)) return cudaErrorInvalidValue;
     if (!key && a.ticks > 0 && !a.host_head && !a.host_rng) {
         int dev = 0, sms = 0;
         cudaGetDevice(&dev);
@@ -954,7 +959,7 @@ cudaError_t launch_merge(cudaStream_t s, const uint32_t* a_key, const uint32_t* 
                          const uint32_t* b_val, const uint32_t* counts, uint32_t* split, uint32_t n,
                          uint32_t* out_key, uint32_t* out_val, const float2* pos, float2* sorted_pos,
                          uint32_t* kstart, uint32_t num_keys, uint4* chunks, uint32_t* chunk_count, uint32_t* err,
-                         uint32_t* kernels, bool chunk_count_zeroed) {
+                         uint32_t* kernels, bool chunk_count_zeroed, uint32_t* rank) {
     if (kernels) *kernels = 0;
     if (n == 0 || num_keys == 0) return cudaSuccess;
     const uint32_t tiles = merge_tiles(n);
@@ -967,7 +972,7 @@ cudaError_t launch_merge(cudaStream_t s, const uint32_t* a_key, const uint32_t* 
                            static_cast<const uint32_t*>(err));
     if (e == cudaSuccess)
         e = launch_chained(k_merge, tiles, kMergeThreads, s, a_key, a_val, b_key, b_val, counts, split, n, out_key,
-                           out_val, pos, sorted_pos, kstart, num_keys, chunks, chunk_count, cap, err);
+                           out_val, pos, sorted_pos, kstart, num_keys, chunks, chunk_count, cap, err, rank);
     if (e != cudaSuccess) return e;
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);

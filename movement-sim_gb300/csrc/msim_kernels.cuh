@@ -63,6 +63,10 @@ struct StepLaunch {
     // non-finite displacement counts as +inf).
     const float2* index_pos = nullptr;
     uint32_t* disp_max = nullptr;
+    // One move tick (move-only kernel): each moved position is also written to
+    // rank_pos[rank[slot]] (its place in a sorted order; ranks >= n are skipped).
+    const uint32_t* rank = nullptr;
+    float2* rank_pos = nullptr;
 };
 
 cudaError_t launch_init_entities(cudaStream_t s, const DeviceMap& m, EntityState st, uint32_t n,
@@ -126,7 +130,8 @@ cudaError_t launch_merge(cudaStream_t s, const uint32_t* a_key, const uint32_t* 
                          const uint32_t* b_val, const uint32_t* counts, uint32_t* split, uint32_t n,
                          uint32_t* out_key, uint32_t* out_val, const float2* pos, float2* sorted_pos,
                          uint32_t* kstart, uint32_t num_keys, uint4* chunks, uint32_t* chunk_count, uint32_t* err,
-                         uint32_t* kernels, bool chunk_count_zeroed = false);
+                         uint32_t* kernels, bool chunk_count_zeroed = false,
+                         uint32_t* rank = nullptr);  // rank (may be NULL): rank[out_val[p]] = p
 // out[q] = pos[P[q]] for the q whose slot P[q] lies in [lo, lo + cnt) (q < n; the
 // other entries are left as they are): the positions of one uploaded chunk of a host
 // tick copied to their places in the sorted order P.

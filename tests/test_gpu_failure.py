@@ -116,11 +116,12 @@ def test_wait_timeout_with_index_reuse(msim, orc):
 
 
 @pytest.mark.parametrize("reuse,arg", [(False, 0), (False, 1), (False, 2), (False, 4), (False, 7),
-                                       (True, 0), (True, 1), (True, 2), (True, 5)])
+                                       (True, 0), (True, 1), (True, 2), (True, 3)])
 def test_injected_launch_failure(msim, orc, reuse, arg):
     """The (arg+1)-th launch of a 2-tick neighbour step fails on the host; the caller
     restores its state with msim_set_entities and continues bit-exact.  Without index
-    reuse both ticks update the index; with it both reuse it (move, gather, query)."""
+    reuse both ticks update the index; with it both reuse it (the move, placing the
+    positions by the ranks of the last update, then the query)."""
     rm = msim.RoadMap.lattice(32, 4)
     n, cap = 20_000, 16
     ost = _oracle(orc, rm, n)

@@ -24,17 +24,21 @@ def _check(sim, ref, orc, ost, radius, cap, what):
     assert sim.collision_pairs() == opairs
 
 
-@pytest.mark.parametrize("side,n,cap,rng", [(48, 200_000, 16, "pcg32"), (16, 100_000, 8, "xorshift128")])
-def test_reuse_matches_oracle_every_tick(msim, orc, side, n, cap, rng):
+@pytest.mark.parametrize("side,n,cap,rng,index", [(48, 200_000, 16, "pcg32", "auto"),
+                                                  (16, 100_000, 8, "xorshift128", "auto"),
+                                                  (48, 200_000, 16, "xorshift128", "full")])
+def test_reuse_matches_oracle_every_tick(msim, orc, side, n, cap, rng, index):
     """(48, 200,000): tiles of about 11 m; (16, 100,000): tiles of 2 x reach, so widened
     boxes span three tiles, and about 15 neighbours per entity (beyond the eight kept
     in registers).  Calls of 1 to 5 ticks (the query of a tick overlaps the next tick),
     re-ordering every 5 ticks, move-only steps in between, then road factors up to 2
-    (a larger bound, so fewer ticks reuse the index)."""
+    (a larger bound, so fewer ticks reuse the index).  With incremental updates the
+    moves of reusing ticks place the positions by the update's ranks; with full sorts
+    (no ranks) a gather pass does."""
     road_map = msim.RoadMap.lattice(side, 7)
     rk = {"xorshift128": 0, "pcg32": 1}[rng]
     radius, dt = 2.0, 0.1
-    kw = dict(rng=rng, dt=dt, radius=radius, cap=cap, resort_interval=5)
+    kw = dict(rng=rng, dt=dt, radius=radius, cap=cap, resort_interval=5, index=index)
     with msim.Simulation(road_map, n, **kw) as sim, msim.Simulation(road_map, n, reuse=False, **kw) as ref:
         for s in (sim, ref):
             s.init_entities(3, placement="fraction", speed=(1.0, 1.6))
