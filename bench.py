@@ -194,8 +194,9 @@ class ClockSampler:
                 "power_w_max": max(r[2] for r in rows), "samples": len(rows), "reasons": sorted(reasons)}
 
 
-def make_sim(pkg, cfg, road_map):
-    sim = pkg.Simulation(road_map, cfg["entities"], rng="pcg32", dt=DT, radius=cfg["radius"], cap=cfg["cap"])
+def make_sim(pkg, cfg, road_map, reuse=True):
+    sim = pkg.Simulation(road_map, cfg["entities"], rng="pcg32", dt=DT, radius=cfg["radius"], cap=cfg["cap"],
+                         reuse=reuse)
     sim.init_entities(SEED, placement="fraction", speed=SPEED)
     return sim
 
@@ -294,6 +295,23 @@ def run_ours(args, cfg, world, rank, local):
         e2e = run_e2e(pkg, sim, cfg, n, nbr, world, min(args.steps, args.e2e_steps))
     sim.close()
 
+    # the same timed window with the index updated on every neighbour tick
+    # (MSIM_PARAM_NO_REUSE): what index reuse is worth on this workload
+    reuse = None
+    if nbr:
+        s2 = make_sim(pkg, cfg, road_map, reuse=False)
+        s2.step(args.warmup, neighbours=True)
+        s2.sync()
+        barrier_sync(world)
+        s2.timer_begin()
+        s2.step(args.steps, neighbours=True)
+        ms2 = max_over_ranks(s2.timer_end(), world)
+        s2.sync()
+        s2.close()
+        reuse = {"index_updates_per_tick": round(sort["index_updates"] / prof_steps, 4),
+                 "without_reuse": {"ms_per_step": ms2 / args.steps,
+                                   "value": world * n * args.steps / (ms2 / 1e3), "index_updates_per_tick": 1.0}}
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         cpu = cpu_baseline(cfg, budget_s=args.cpu_budget)
@@ -301,7 +319,7 @@ def run_ours(args, cfg, world, rank, local):
         "value": value, "ms_per_step": ms_max / args.steps, "clocks": clocks.summary(), "k_mean": k_mean,
         "roofline": roofline, "roofline_tick": roofline_tick, "kernels": kernels, "e2e": e2e, "cpu": cpu,
         "launches": launches, "info": info, "roads": road_map.num_roads, "config_run": config_run,
-        "sorted_fraction": sorted_per_update / max(n, 1),
+        "sorted_fraction": sorted_per_update / max(n, 1), "reuse": reuse,
     }
 
 
@@ -798,7 +816,8 @@ def main():
                                "cell_m": round(r["info"]["cell_size"], 3), "sort_passes": r["info"]["sort_passes"],
                                "resort_interval": r["info"]["resort_interval"],
                                "mean_kept_neighbours": round(r["k_mean"], 4),
-                               "sorted_fraction_per_tick": round(r["sorted_fraction"], 5)},
+                               "sorted_fraction_per_update": round(r["sorted_fraction"], 5),
+                               "reuse": r["reuse"]},
                      "kernels": {k: {kk: (round(vv, 5) if isinstance(vv, float) else vv) for kk, vv in v.items()}
                                  for k, v in r["kernels"].items()}})
         if forms is not None:
