@@ -50,10 +50,14 @@ ADJ_FWD_BYTES = B_STEP + 8
 ADJ_BWD_BYTES = B_STEP + 8 + 16
 
 
-def b_nbr(k_mean: float) -> float:
-    """Algorithmic bytes per entity of a neighbour tick: (key, id) write 8, sort
-    read 8 + sorted write 8, query read 8, count write 4, 4 per kept neighbour."""
-    return 36.0 + 4.0 * k_mean
+def b_nbr(k_mean: float, updates_per_tick: float = 1.0) -> float:
+    """Algorithmic bytes per entity of a neighbour tick.  A tick that updates the
+    index: (key, id) write 8, sort read 8 + sorted write 8, query read 8, count write
+    4, 4 per kept neighbour (36 + 4k).  A tick that reuses the index: sorted-position
+    write 8, query read 8, count write 4, 4 per kept neighbour (20 + 4k).  Mixed by
+    the measured share of updating ticks."""
+    u = min(max(updates_per_tick, 0.0), 1.0)
+    return 20.0 + 16.0 * u + 4.0 * k_mean
 
 
 # per-kernel algorithmic bytes per entity and launch: the per-entity figures of a
@@ -283,10 +287,12 @@ def run_ours(args, cfg, world, rank, local):
     ach = dominant[1]["achieved_gbs"] or 0.0
     roofline = {"bound": "hbm", "kernel": dominant[0], "achieved": round(ach, 1), "peak": peak, "unit": "GB/s",
                 "frac": round(ach / peak, 4), "traffic": traffic, "peak_source": peak_kind}
-    tick_bytes = (B_STEP + (b_nbr(k_mean) if nbr else 0.0)) * n
+    updates_per_tick = sort["index_updates"] / prof_steps if nbr else 0.0
+    tick_bytes = (B_STEP + (b_nbr(k_mean, updates_per_tick) if nbr else 0.0)) * n
     tick_gbs = tick_bytes * args.steps / (ms / 1e3) / 1e9
     roofline_tick = {"achieved": round(tick_gbs, 1), "peak": peak, "unit": "GB/s", "frac": round(tick_gbs / peak, 4),
-                     "algo_bytes_per_entity_step": B_STEP + (b_nbr(k_mean) if nbr else 0.0)}
+                     "algo_bytes_per_entity_step": round(tick_bytes / n, 3),
+                     "index_updates_per_tick": round(updates_per_tick, 4)}
 
     # end to end through the C ABI with host buffers: upload the entity state from
     # pinned memory, run one tick, read the state and neighbour counts back

@@ -94,3 +94,30 @@ def test_reuse_off_when_steps_are_large(msim, orc):
             ocnt, oidx, _ = orc.neighbours(ost[0], 1.0, 8, threads=8)
             assert np.array_equal(cnt, ocnt) and np.array_equal(idx, oidx), f"neighbours differ at tick {t + 1}"
         assert sim.sort_stats()["index_updates"] - u0 == 6
+
+
+def test_reuse_far_from_the_map(msim, orc):
+    """Entities set 50 km away from a 0.8 km map (positions with an ulp of 4 mm), in a
+    cluster a few metres across, heading back to their roads: the bound's rounding
+    term follows the largest coordinate, and the reused index stays exact."""
+    road_map = msim.RoadMap.lattice(16, 4)
+    n = 20_000
+    rs = np.random.default_rng(9)
+    with msim.Simulation(road_map, n, rng="pcg32", dt=0.1, radius=2.0, cap=16) as sim:
+        sim.init_entities(2, placement="fraction", speed=(1.0, 1.6))
+        st = sim.get_state()
+        pos = (np.float32([50_000.0, -30_000.0]) + rs.uniform(-15.0, 15.0, (n, 2))).astype(np.float32)
+        sim.set_entities(pos, st["heading"], st["rng"], st["speed"])
+        ost = [pos.copy(), st["heading"].copy(), st["rng"].copy(), st["speed"].copy()]
+        u0 = sim.sort_stats()["index_updates"]
+        for t in range(30):
+            sim.step(1, neighbours=True)
+            orc.step(road_map.road_pos, road_map.road_conn, road_map.connections, ost[0], ost[1], ost[2], ost[3], 1,
+                     0.1, 1, threads=8)
+            got = sim.get_state()
+            assert np.array_equal(got["pos"].view(np.uint32), ost[0].view(np.uint32)), f"positions differ at {t + 1}"
+            cnt, idx = sim.get_neighbours()
+            ocnt, oidx, _ = orc.neighbours(ost[0], 2.0, 16, threads=8)
+            assert np.array_equal(cnt, ocnt) and np.array_equal(idx, oidx), f"neighbours differ at tick {t + 1}"
+        assert ocnt.sum() > n  # a crowd: the widened boxes matter
+        assert sim.sort_stats()["index_updates"] - u0 < 30
