@@ -727,10 +727,11 @@ int neighbour_tick(msim_ctx* c) {
     int rc;
     if (c->tick_timing) CK(cudaEventRecord(c->ev_tick[0], c->stream), "cudaEventRecord");
     // Index reuse: while the widening of this tick's boxes stays within kWidenLimit of
-    // the reach, the tick moves the entities, gathers their positions into the index's
-    // sorted order and queries the index built reuse_ticks + 1 ticks before; the
-    // widening costs little of the query (16 M, reach 2 m + 0.49 m: 0.390 ms against
-    // 0.385), the update it skips (split, passes, merge) about 0.30 ms.
+    // the reach, the tick moves the entities (each position also written at its sorted
+    // position in the index, by the ranks of the last update, or gathered there after
+    // a full sort) and queries the index built reuse_ticks + 1 ticks before; the
+    // widening costs about 10 % of the query over a reuse window at 16 M (0.40 ms
+    // against 0.36-0.39), the update it skips (split, passes, merge) about 0.30 ms.
     const double ticks = c->reuse_ticks >= 0 ? (double)c->reuse_ticks + 1.0 : 0.0;
     bool reuse = false;
     if (c->reuse && c->sorted_key && !c->order_identity && c->reuse_ticks >= 0 && c->grid.reach > 0.f &&
