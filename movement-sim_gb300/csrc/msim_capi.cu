@@ -373,6 +373,19 @@ EntityState& cur_state(msim_ctx* c) { return c->st[c->cur]; }
 // 17 or 70 neighbours it costs the same at 0 and 1.0 (1.41 and 22.4 ms at 1 M).
 constexpr float kWidenLimit = 1.0f;
 
+// rank[slot] (written by every later merge once allocated): false when the allocation
+// fails.
+bool ensure_rank(msim_ctx* c) {
+    if (c->rank) return true;
+    void* raw = nullptr;
+    if (!device_malloc(&raw, sizeof(uint32_t) * std::max<size_t>(c->n, 1))) return false;
+    c->allocs.push_back(raw);
+    c->device_bytes += sizeof(uint32_t) * std::max<size_t>(c->n, 1);
+    c->rank = static_cast<uint32_t*>(raw);
+    c->rank_valid = false;
+    return true;
+}
+
 // Buffers of the skin query (allocated by the first host tick that can use it): false
 // when an allocation fails, and the tick then takes the usual order.
 bool ensure_skin(msim_ctx* c) {
@@ -405,14 +418,7 @@ bool ensure_skin(msim_ctx* c) {
 // Buffers of index reuse on the device path (allocated by the first reusing tick):
 // false when an allocation fails, and the ticks then update the index every time.
 bool ensure_reuse(msim_ctx* c) {
-    if (!c->rank) {
-        void* raw = nullptr;
-        if (!device_malloc(&raw, sizeof(uint32_t) * std::max<size_t>(c->n, 1))) return false;
-        c->allocs.push_back(raw);
-        c->device_bytes += sizeof(uint32_t) * std::max<size_t>(c->n, 1);
-        c->rank = static_cast<uint32_t*>(raw);
-        c->rank_valid = false;
-    }
+    if (!ensure_rank(c)) return false;
     for (int b = 0; b < 2; b++) {
         if (!c->reuse_pos[b]) {
             void* raw = nullptr;
@@ -614,7 +620,7 @@ int build_index(msim_ctx* c) {
 // table and the sorted positions on the way).  The update's scratch (digit counts,
 // split ticket and look-back words) is cleared first, in one memset, before the
 // move, so that the move step and the split run back to back.
-int incremental_update(msim_ctx* c, bool positions = true);
+int incremental_update(msim_ctx* c, bool positions = true, bool ranks = true);
 
 int clear_update_scratch(msim_ctx* c) {
     CK(cudaMemsetAsync(c->hist, 0, sizeof(uint32_t) * c->update_words, c->stream), "memset update scratch");
@@ -641,8 +647,11 @@ int incremental_index(msim_ctx* c) {
 
 // The update itself, for new keys (by slot) already in c->key.  positions = false:
 // the sorted positions are not written (a host tick whose next query reads the
-// positions it gathers itself).
-int incremental_update(msim_ctx* c, bool positions) {
+// positions it gathers itself).  ranks = false: no ranks either (a host tick's slots
+// are entity ids, in no spatial order: writing rank[slot] scatters at random, 0.12 ms
+// more per update at 16 M, and moves placing positions by them cost 0.11 ms more per
+// 4 M chunk than the gather passes).
+int incremental_update(msim_ctx* c, bool positions, bool ranks) {
     NvtxRange range("msim index update");
     int rc = inject_sort_tile(c, c->mark_ticket);
     if (rc != MSIM_OK) return rc;
@@ -680,9 +689,9 @@ int incremental_update(msim_ctx* c, bool positions) {
                         c->ab_counts, c->merge_split, c->n, c->sk[out], c->sv[out],
                         positions ? cur_state(c).pos : nullptr, positions ? c->sorted_pos : nullptr,
                         c->kstart, (uint32_t)c->num_keys, c->kstart_chunks, c->kstart_chunk_count, c->err,
-                        &launched, c->chunk_count_zeroed, c->rank),
+                        &launched, c->chunk_count_zeroed, ranks ? c->rank : nullptr),
            "k_merge");
-        c->rank_valid = c->rank != nullptr;
+        c->rank_valid = ranks && c->rank != nullptr;
         c->chunk_count_zeroed = false;
         if (launched > 1) c->launch_count += launched - 1;
     }
@@ -770,6 +779,7 @@ int neighbour_tick(msim_ctx* c) {
         if (c->rank_valid) {
             a.rank = c->rank;
             a.rank_pos = c->reuse_pos[x];
+            a.rank_n = c->n;
         }
         CKL(p, launch_step(c->stream, a), "k_step");
     }
@@ -1338,7 +1348,8 @@ int msim_tick_host(msim_ctx* c, const float* in_pos, const uint32_t* in_heading,
         CK(cudaEventRecord(c->ev_up[k], c->up), "cudaEventRecord");
         CK(cudaStreamWaitEvent(c->stream, c->ev_up[k], 0), "cudaStreamWaitEvent");
         if (!in_speed) CK(launch_fill(c->stream, s.speed + lo, cnt, 1.4f), "k_fill");  // SPEED, random_move.comp:750
-        CK(launch_check_roads_range(c->stream, s.head, lo, cnt, c->R, c->check), "k_check_roads");
+        if (!skin)  // (the skin path's move checks the headings itself)
+            CK(launch_check_roads_range(c->stream, s.head, lo, cnt, c->R, c->check), "k_check_roads");
         {
             Prof p(c, K_STEP);
             StepLaunch a = step_args(c, 1, nbr);
@@ -1357,6 +1368,7 @@ int msim_tick_host(msim_ctx* c, const float* in_pos, const uint32_t* in_heading,
             if (skin) {  // displacement against the positions the current index was built from
                 a.index_pos = c->st[old].pos + lo;
                 a.disp_max = c->disp;
+                a.first_bad = c->check;
             }
             CK(launch_step(c->stream, a), "k_step");
         }
@@ -1439,7 +1451,7 @@ int msim_tick_host(msim_ctx* c, const float* in_pos, const uint32_t* in_heading,
         dl = c->down;
     } else if (nbr) {
         if (use_inc) {
-            if ((rc = incremental_update(c)) != MSIM_OK) return rc;
+            if ((rc = incremental_update(c, true, false)) != MSIM_OK) return rc;
         } else {
             reset_index(c);
             if ((rc = sort_keys(c)) != MSIM_OK || (rc = key_start_table(c)) != MSIM_OK) return rc;
@@ -1462,7 +1474,7 @@ int msim_tick_host(msim_ctx* c, const float* in_pos, const uint32_t* in_heading,
            "download neighbours");
     // the index of the new state for the next call (no sorted positions: its query
     // gathers its own); with the skin query this runs after the query, off the host's path
-    if (nbr && skin && (rc = incremental_update(c, false)) != MSIM_OK) return rc;
+    if (nbr && skin && (rc = incremental_update(c, false, false)) != MSIM_OK) return rc;
     c->tick++;
     uint32_t first_bad = 0;
     // read after the query: the heading checks of every chunk ran before it

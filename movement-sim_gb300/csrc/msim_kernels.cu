@@ -186,7 +186,7 @@ __global__ __launch_bounds__(kMoveThreads) void k_move(StepLaunch a) {
         if (rd) a.st.rng[s] = r;
         if (a.rank_pos) {  // uniform: a tick that reuses the index
             const uint32_t q = a.rank[s];
-            if (q < a.n) a.rank_pos[q] = p;
+            if (q < a.rank_n) a.rank_pos[q] = p;
         }
     }
 }
@@ -230,6 +230,8 @@ __global__ __launch_bounds__(kStepThreads, 4) void k_step(StepLaunch a) {
                 if (a.ticks) {
                     h[u] = h0[u] = a.st.head[sl[u]];
                     sp[u] = a.st.speed[sl[u]];
+                    if (DISP && a.first_bad && (h[u] & kHeadRoad) >= a.map.num_roads)
+                        atomicMin(a.first_bad, a.id_base + sl[u]);
                 }
             }
         }

@@ -63,10 +63,15 @@ struct StepLaunch {
     // non-finite displacement counts as +inf).
     const float2* index_pos = nullptr;
     uint32_t* disp_max = nullptr;
+    // With disp_max: the first entity (id_base + slot) whose heading names a road out of
+    // range is atomically min-ed into *first_bad (NULL: not checked here).
+    uint32_t* first_bad = nullptr;
     // One move tick (move-only kernel): each moved position is also written to
-    // rank_pos[rank[slot]] (its place in a sorted order; ranks >= n are skipped).
+    // rank_pos[rank[slot]] (its place in a sorted order of rank_n entries; larger ranks
+    // are skipped).
     const uint32_t* rank = nullptr;
     float2* rank_pos = nullptr;
+    uint32_t rank_n = 0;
 };
 
 cudaError_t launch_init_entities(cudaStream_t s, const DeviceMap& m, EntityState st, uint32_t n,

@@ -270,3 +270,39 @@ def test_skin_query_matches_oracle(msim, orc, side, n, cap, rng):
             state = {"pos": got["pos"].copy(), "heading": got["heading"].copy(), "rng": got["rng"].copy(),
                      "speed": state["speed"]}
         assert sim.host_tick_stats()["skin_queries"] == skin + 2  # the first after the regular ticks sorts
+
+
+def test_bad_heading_on_the_skin_path(msim, orc):
+    """A bad heading in a host tick that takes the skin path (its move checks the
+    headings itself): MSIM_ERR_OOB naming the first bad entity, the context's state
+    kept, and the host ticks after it match the oracle."""
+    road_map = msim.RoadMap.lattice(24, 6)
+    n = 150_000
+    with msim.Simulation(road_map, n, rng="pcg32", dt=0.1, radius=2.0, cap=8, index="incremental") as sim:
+        sim.init_entities(4, placement="fraction", speed=(1.0, 1.6))
+        st = sim.get_state()
+        state = {k: st[k].copy() for k in ("pos", "heading", "rng", "speed")}
+        for _ in range(2):
+            got = sim.tick_host(state, neighbours=True)
+            state = {"pos": got["pos"].copy(), "heading": got["heading"].copy(), "rng": got["rng"].copy(),
+                     "speed": state["speed"]}
+        assert sim.host_tick_stats()["skin_queries"] == 1
+        before = sim.get_state()
+        bad = {k: v.copy() for k, v in state.items()}
+        bad["heading"][[140_001, 70_123]] = road_map.num_roads + 5  # chunks 3 and 2
+        with pytest.raises(msim.MsimError) as e:
+            sim.tick_host(bad, neighbours=True)
+        assert e.value.code == 2 and "70123" in str(e.value)
+        after = sim.get_state()
+        for k in before:
+            assert np.array_equal(before[k], after[k])
+        pos, head, rng = state["pos"].copy(), state["heading"].copy(), state["rng"].copy()
+        for t in range(3):
+            got = sim.tick_host(state, neighbours=True)
+            orc.step(road_map.road_pos, road_map.road_conn, road_map.connections, pos, head, rng, state["speed"], 1,
+                     0.1, 1, threads=8)
+            _same_state(got, {"pos": pos, "heading": head, "rng": rng}, f"at host tick {t + 1} after the error")
+            ocnt, _, _ = orc.neighbours(pos, 2.0, 8, threads=8, with_idx=False)
+            assert np.array_equal(got["count"], ocnt), f"counts differ at host tick {t + 1} after the error"
+            state = {"pos": got["pos"].copy(), "heading": got["heading"].copy(), "rng": got["rng"].copy(),
+                     "speed": state["speed"]}
