@@ -83,6 +83,11 @@ KERNEL_BYTES = {
 # ncu capture (405.8 M for 64 instances, 2,058,939 entities, 100 ticks, tuned
 # schedule; profiles/batched_64_instances_k_batch_step_issue.md) over entities x ticks
 NCU_BATCH_WARP_INSTR_PER_ENTITY_STEP = 1.971
+# warp instructions per entity of k_query on a reused index (widened boxes):
+# smsp__inst_executed.sum of one ncu capture (96.2 M for 4,000,000 entities on the
+# 512 x 512 lattice, the 16 M and 1 M workloads' density;
+# profiles/mid_4M_k_query_widened_ncu.md)
+NCU_QUERY_WARP_INSTR_PER_ENTITY = 24.04
 
 NCU_DRAM_BYTES_PER_ENTITY = {
     "scale": {"k_query": 26.87, "k_merge": 32.78, "k_mark": 16.91, "k_step": 27.98},
@@ -287,6 +292,18 @@ def run_ours(args, cfg, world, rank, local):
     ach = dominant[1]["achieved_gbs"] or 0.0
     roofline = {"bound": "hbm", "kernel": dominant[0], "achieved": round(ach, 1), "peak": peak, "unit": "GB/s",
                 "frac": round(ach / peak, 4), "traffic": traffic, "peak_source": peak_kind}
+    # The query is bound by instruction issue (its algorithmic bytes are a small part of
+    # what it does): warp instructions per entity (ncu) x entities per launch / launch
+    # time, against one warp instruction per cycle on each of the 4 schedulers of the
+    # 152 SMs at the sampled SM clock.
+    if dominant[0] == "k_query" and args.config in ("scale", "neighbours") and \
+            not any(getattr(args, k) is not None for k in ("entities", "lattice", "cap")):
+        sm_mhz = clocks.summary().get("sm_mhz") or 2070.0
+        issue_peak = 152 * 4 * sm_mhz * 1e6
+        inst_s = NCU_QUERY_WARP_INSTR_PER_ENTITY * n / (dominant[1]["avg_ms"] / 1e3)
+        roofline["issue"] = {"bound": "issue", "achieved": round(inst_s, 1), "peak": issue_peak,
+                             "unit": "warp-instructions/s", "frac": round(inst_s / issue_peak, 4),
+                             "warp_instructions_per_entity": NCU_QUERY_WARP_INSTR_PER_ENTITY, "sm_mhz": sm_mhz}
     updates_per_tick = sort["index_updates"] / prof_steps if nbr else 0.0
     tick_bytes = (B_STEP + (b_nbr(k_mean, updates_per_tick) if nbr else 0.0)) * n
     tick_gbs = tick_bytes * args.steps / (ms / 1e3) / 1e9
