@@ -352,7 +352,8 @@ void Simulator::write_log_csv_file(uint64_t tick, std::chrono::nanoseconds updat
     std::tm tm{};
     gmtime_r(&secs, &tm);
     char stamp[32];
-    std::snprintf(stamp, sizeof(stamp), "%02d:%02d:%02d.%03lld", tm.tm_hour, tm.tm_min, tm.tm_sec, ms % 1000);
+    std::snprintf(stamp, sizeof(stamp), "%02d:%02d:%02d.%03lld", tm.tm_hour, tm.tm_min, tm.tm_sec,
+                  static_cast<long long>(ms % 1000));
     char line[160];
     std::snprintf(line, sizeof(line), "%s;%llu;%.6f;%.6f;%.6f\n", stamp, static_cast<unsigned long long>(tick),
                   update.count() / 1e9, collision.count() / 1e9, all.count() / 1e9);
