@@ -72,6 +72,7 @@ KERNEL_BYTES = {
                                            # (+ 4 B per key slot, added below)
     "k_query": lambda k: 12 + 4 * k,       # own pos 8 + count 4 + kept ids
     "k_gather": lambda k: 20,              # order read 4, position read 8 + write 8
+    "k_move": lambda k: B_STEP + 12,       # reusing tick: move + rank read 4 + placed position write 8
     "k_permute": lambda k: 72,             # 36-byte state read + write
     "k_step_multi": lambda k: B_STEP,      # per tick
 }

@@ -56,11 +56,12 @@ enum KernelId : uint32_t {
     K_MARK,   // split of the previous order into unchanged / changed keys
     K_MERGE,  // merge + key-start table + sorted positions
     K_GATHER, // host tick: an uploaded chunk's positions into the previous sorted order
+    K_MOVE,   // a tick that reuses the index: move + each position at its sorted position
     K_COUNT
 };
 static const char* const kKernelNames[K_COUNT] = {"k_init",   "k_step",   "k_step_multi", "k_onesweep",
                                                   "k_kstart", "k_query",  "k_permute",    "k_export",
-                                                  "k_mark",   "k_merge",  "k_gather"};
+                                                  "k_mark",   "k_merge",  "k_gather", "k_move"};
 
 // msim_tick_host: at most this many chunks, each at least kHostChunkMin entities
 constexpr uint32_t kHostChunks = 4;  // at 16 M: 4.09 ms per host tick; 8 chunks 4.16-4.18, 16 4.31
@@ -774,7 +775,7 @@ int neighbour_tick(msim_ctx* c) {
         c->reuse_read_pending[x] = false;
     }
     {  // the move writes each position at its sorted position too, when the ranks are known
-        Prof p(c, K_STEP);
+        Prof p(c, K_MOVE);
         StepLaunch a = step_args(c, 1, false);
         if (c->rank_valid) {
             a.rank = c->rank;
